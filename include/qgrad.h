@@ -1,0 +1,134 @@
+/*
+ * qgrad: C ABI of the GB300-native statevector run / adjoint grad_run path
+ * of qradient's McClean and QAOA circuits.
+ *
+ * The reference (frederikwilde/qradient) is pure Python; it has no FFI.  Its
+ * drop-in boundary is the circuit_logic class API, and every entry point here
+ * is what a Python (ctypes) binding of that API calls:
+ *
+ *   qg_mcclean_create  <- McClean.__init__       qradient/circuit_logic/mc_clean.py:9-25
+ *                         (+ Observable matrix   qradient/physical_components/observable.py:34-73)
+ *   qg_qaoa_create     <- Qaoa.__init__          qradient/circuit_logic/qaoa.py:9-21
+ *   qg_run             <- McClean.run_expec_val  qradient/circuit_logic/mc_clean.py:27-45
+ *                         Qaoa.run_expec_val     qradient/circuit_logic/qaoa.py:23-38
+ *   qg_grad            <- McClean.grad_run       qradient/circuit_logic/mc_clean.py:47-78
+ *                         Qaoa.grad_run          qradient/circuit_logic/qaoa.py:40-70
+ *   qg_maxcut_table    <- State.load_classical_ham (its diagonal)
+ *                                                qradient/physical_components/state.py:261-297
+ *   qg_sample          <- Qaoa.__sample          qradient/circuit_logic/qaoa.py:196-198
+ *
+ * Conventions
+ *   - Qubit q is bit (n-1-q) of the basis index (state.py:84-88).
+ *   - States are interleaved complex arrays: complex128 (QG_C128) or
+ *     complex64 (QG_C64), 2^n elements.
+ *   - Every pointer argument of qg_run / qg_grad / qg_sample /
+ *     qg_maxcut_table named *_dev is device memory; the caller owns all device
+ *     buffers.  The library allocates no device memory: scratch lives in the
+ *     caller's workspace, sized by qg_workspace_size.
+ *   - Calls are ordered on the given stream; a circuit handle is immutable
+ *     after creation and may be used from several threads on distinct streams
+ *     and workspaces.
+ *   - Errors are returned as status codes (never traps); qg_last_error()
+ *     gives a message for the calling thread.
+ */
+#ifndef QGRAD_H
+#define QGRAD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qg_circuit qg_circuit;
+typedef struct CUstream_st* qg_stream; /* cudaStream_t */
+
+enum qg_status {
+  QG_OK = 0,
+  QG_ERR_INVALID = 1,     /* bad argument; the reference raises ValueError here */
+  QG_ERR_CUDA = 2,        /* a CUDA call failed; see qg_last_error() */
+  QG_ERR_WORKSPACE = 3,   /* workspace too small */
+  QG_ERR_UNSUPPORTED = 4, /* valid request outside this build's limits */
+  QG_ERR_HOST_MEMORY = 5
+};
+
+enum qg_dtype { QG_C128 = 0, QG_C64 = 1 };
+
+/* Entangler of a McClean layer.  QG_ENT_CNOT_LADDER is the reference's
+ * ladder (state.py:209-251): CNOT(q, q+1) on odd q, then on even q. */
+enum qg_entangler { QG_ENT_NONE = 0, QG_ENT_CNOT_LADDER = 1, QG_ENT_CZ_LADDER = 2 };
+/* Where the entangler sits in a layer.  The reference applies it before the
+ * rotations (mc_clean.py:58-62). */
+enum qg_placement { QG_PLACE_BEFORE = 0, QG_PLACE_AFTER = 1 };
+
+enum qg_pauli { QG_PAULI_X = 0, QG_PAULI_Y = 1, QG_PAULI_Z = 2, QG_PAULI_ZZ = 3 };
+
+/* qg_grad strategies: keep every intermediate state (fewest operations,
+ * memory ~ (sweeps + 2) states) or uncompute psi backwards (3 states). */
+enum qg_op { QG_OP_RUN = 0, QG_OP_GRAD_HISTORY = 1, QG_OP_GRAD_UNCOMPUTE = 2 };
+
+/* McClean.__init__ (mc_clean.py:9-25) with the observable dict flattened to
+ * terms (observable.py:12-17): term k is kind[k] in qg_pauli on qubit q0[k]
+ * (and q1[k] > q0[k] for ZZ) with weight w[k].  axes is host int32 [L*n]
+ * with values 0 (X), 1 (Y), 2 (Z) (mc_clean.py:383-392).  Angles are passed
+ * per call.  All arrays are host memory. */
+int qg_mcclean_create(int n, int layers, const int32_t* axes, int entangler, int placement, int nterms,
+                      const int32_t* kind, const int32_t* q0, const int32_t* q1, const double* w, qg_circuit** out);
+
+/* Qaoa.__init__ (qaoa.py:9-21): the observable's Z and ZZ terms form the
+ * classical cost C (state.py:261-297); X and Y terms only enter qg_run's
+ * expectation value, as in the reference (base.py:17-20). */
+int qg_qaoa_create(int n, int layers, int nterms, const int32_t* kind, const int32_t* q0, const int32_t* q1,
+                   const double* w, qg_circuit** out);
+
+void qg_destroy(qg_circuit* c);
+
+/* Number of parameters: McClean L*n (angles [L, n] row-major); QAOA 2p
+ * (params [p, 2] row-major: column 0 beta, column 1 gamma, the grad layout
+ * of qaoa.py:46). */
+int qg_num_params(const qg_circuit* c, int* nparams);
+
+/* Device workspace bytes for an operation (qg_op) at a dtype. */
+int qg_workspace_size(const qg_circuit* c, int dtype, int op, size_t* bytes);
+
+/* Forward run and exact expectation value <psi|O|psi> (run_expec_val with
+ * exact_expec_val=True).  params_dev: double [nparams].  ini_state_dev:
+ * optional start state (NULL: |0..0> for McClean, |+..+> for QAOA); McClean
+ * still applies its Ry(pi/4) layer to it (mc_clean.py:29-36).  expec_dev:
+ * one double.  state_out_dev: optional, receives the final state. */
+int qg_run(const qg_circuit* c, int dtype, const double* params_dev, const void* ini_state_dev, void* workspace_dev,
+           size_t workspace_bytes, double* expec_dev, void* state_out_dev, qg_stream stream);
+
+/* Adjoint gradient (grad_run): expec_dev receives E, grad_dev the nparams
+ * derivatives.  op is QG_OP_GRAD_HISTORY or QG_OP_GRAD_UNCOMPUTE. */
+int qg_grad(const qg_circuit* c, int dtype, int op, const double* params_dev, const void* ini_state_dev,
+            void* workspace_dev, size_t workspace_bytes, double* expec_dev, double* grad_dev, qg_stream stream);
+
+/* Integer MaxCut / ZZ cost table: table_dev[x] = sum over edges (i, j) of
+ * z_i z_j with z = +1 for bit 0 (state.py:280-292 with unit weights).
+ * edges: host int32 [nedges, 2]. */
+int qg_maxcut_table(int n, int nedges, const int32_t* edges, int32_t* table_dev, qg_stream stream);
+
+/* Draw nshots basis indices from |psi|^2 (Qaoa.__sample, qaoa.py:196-198)
+ * with a counter-based Philox4x32-10 stream (seed, offset).  Returns indices
+ * in out_dev (int64 [nshots]).  Needs qg_sample_workspace_size bytes. */
+int qg_sample_workspace_size(int n, size_t* bytes);
+int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t seed, uint64_t offset,
+              void* workspace_dev, size_t workspace_bytes, int64_t* out_dev, qg_stream stream);
+
+/* Measured FP64 FMA issue rate of this GPU (FMA/s), for roofline
+ * reporting: a dependent-chain DFMA kernel timed with CUDA events.
+ * scratch_dev needs 1 MiB.  Synchronises the stream. */
+int qg_probe_fp64_fma_rate(void* scratch_dev, size_t scratch_bytes, double* fma_per_s, qg_stream stream);
+
+const char* qg_status_string(int status);
+/* Message of the last failed call on this thread. */
+const char* qg_last_error(void);
+int qg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QGRAD_H */

@@ -1,0 +1,817 @@
+// Sweep kernels: forward gate sweeps, adjoint backward sweeps with fused
+// gradient reductions, the observable pass, and the gradient finaliser.
+//
+// Reference mapping (qradient, pure numpy):
+//   rotations          physical_components/state.py:90-97, 142-149, 168-175
+//   CNOT ladder        physical_components/state.py:209-251
+//   observable         physical_components/observable.py:34-73, base.py:17-20
+//   McClean grad_run   circuit_logic/mc_clean.py:47-78
+//   QAOA grad_run      circuit_logic/qaoa.py:40-70
+#include "qg_internal.cuh"
+#include "qg_kernels.h"
+
+namespace qg {
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ double angle_of(const AngleRef& a, const double* params) {
+  return a.param >= 0 ? (double)a.sign * params[a.param] : a.fixed;
+}
+
+// Reference CNOT ladder as a basis permutation: CNOT(q, q+1) flips bit
+// (n-2-q) when bit (n-1-q) is set, i.e. x ^= (x & bit_c) >> 1.  The odd-pair
+// CNOTs act first, then the even pairs (state.py:235-241).  The pairs of one
+// parity are disjoint, so each parity is one masked shift-xor.
+struct LadderMasks {
+  uint64_t odd, even;
+};
+
+__device__ __forceinline__ LadderMasks ladder_masks(int n) {
+  LadderMasks m{0, 0};
+  for (int q = 0; q + 1 < n; ++q) {
+    const uint64_t b = 1ull << (n - 1 - q);
+    if (q & 1)
+      m.odd |= b;
+    else
+      m.even |= b;
+  }
+  return m;
+}
+
+// A(x): ladder |x> = |A(x)>
+__device__ __forceinline__ uint64_t ladder_fwd(uint64_t x, const LadderMasks& m) {
+  x ^= (x & m.odd) >> 1;
+  x ^= (x & m.even) >> 1;
+  return x;
+}
+// A^{-1}(x)
+__device__ __forceinline__ uint64_t ladder_inv(uint64_t x, const LadderMasks& m) {
+  x ^= (x & m.even) >> 1;
+  x ^= (x & m.odd) >> 1;
+  return x;
+}
+
+// CZ on all neighbouring qubit pairs: (-1)^{popcount(x & (x >> 1))}
+__device__ __forceinline__ bool cz_negative(uint64_t x) { return __popcll(x & (x >> 1)) & 1; }
+
+// Shared-memory swizzle: XOR the low bits of an element index with a
+// function of the next bit, so that the 8 (complex128) or 16 (complex64)
+// elements a quarter/half warp touches in a pair loop over bits 0..2 (0..3)
+// land in distinct banks.
+template <typename R>
+__device__ __forceinline__ int sw(int e);
+template <>
+__device__ __forceinline__ int sw<double>(int e) {
+  return e ^ (((e >> 3) & 1) * 7);
+}
+template <>
+__device__ __forceinline__ int sw<float>(int e) {
+  return e ^ (((e >> 4) & 1) * 15);
+}
+
+__device__ __forceinline__ int insert0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
+
+template <typename C>
+__device__ __forceinline__ C cmul(C a, double2 b);
+template <>
+__device__ __forceinline__ double2 cmul<double2>(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+template <>
+__device__ __forceinline__ float2 cmul<float2>(float2 a, double2 b) {
+  const float bx = (float)b.x, by = (float)b.y;
+  return make_float2(fmaf(a.x, bx, -a.y * by), fmaf(a.x, by, a.y * bx));
+}
+
+template <typename C>
+__device__ __forceinline__ C cscale(C a, double k);
+template <>
+__device__ __forceinline__ double2 cscale<double2>(double2 a, double k) {
+  return make_double2(a.x * k, a.y * k);
+}
+template <>
+__device__ __forceinline__ float2 cscale<float2>(float2 a, double k) {
+  const float kf = (float)k;
+  return make_float2(a.x * kf, a.y * kf);
+}
+
+template <typename C>
+__device__ __forceinline__ C cneg(C a) {
+  a.x = -a.x;
+  a.y = -a.y;
+  return a;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Scaled-form choice for a rotation angle theta (see qg_internal.cuh):
+// returns the multiplier u and sets form (0: [[1, .u],[.u, 1]], 1: [[u, .],[., u]])
+// and the scale factor kappa.
+__device__ __forceinline__ double rot_form(double theta, int* form, double* kappa) {
+  double s, c;
+  sincos(0.5 * theta, &s, &c);
+  if (fabs(c) >= fabs(s)) {
+    *form = 0;
+    *kappa = c;
+    return s / c;
+  }
+  *form = 1;
+  *kappa = s;
+  return c / s;
+}
+
+// Apply one X/Y rotation (scaled form) to the pair (a, b) = (bit 0, bit 1).
+// sg = +1 applies R(theta), sg = -1 applies R(-theta).
+template <typename C, typename R>
+__device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u, R sg) {
+  const C a0 = a, b0 = b;
+  if (axis == AX_X) {
+    // -i * sg applied to the partner: (-i v) = (v.y, -v.x)
+    if (form == 0) {
+      const R us = u * sg;
+      a.x = fma(us, b0.y, a0.x);
+      a.y = fma(-us, b0.x, a0.y);
+      b.x = fma(us, a0.y, b0.x);
+      b.y = fma(-us, a0.x, b0.y);
+    } else {
+      a.x = fma(u, a0.x, sg * b0.y);
+      a.y = fma(u, a0.y, -sg * b0.x);
+      b.x = fma(u, b0.x, sg * a0.y);
+      b.y = fma(u, b0.y, -sg * a0.x);
+    }
+  } else {
+    // Y: [[1, -t],[t, 1]] (form 0) or [[u, -1],[1, u]] (form 1)
+    if (form == 0) {
+      const R us = u * sg;
+      a.x = fma(-us, b0.x, a0.x);
+      a.y = fma(-us, b0.y, a0.y);
+      b.x = fma(us, a0.x, b0.x);
+      b.y = fma(us, a0.y, b0.y);
+    } else {
+      a.x = fma(u, a0.x, -sg * b0.x);
+      a.y = fma(u, a0.y, -sg * b0.y);
+      b.x = fma(u, b0.x, sg * a0.x);
+      b.y = fma(u, b0.y, sg * a0.y);
+    }
+  }
+}
+
+// ------------------------------------------------------------ shared setup
+
+struct SetupShared {
+  double u[TMAX];
+  int form[TMAX];
+  int64_t offhi[32];   // deposit(k << 8) for the element loop
+  uint8_t outside[QMAX];
+  double startP[QMAX + 1];
+  double red[NTHREADS / 32][TMAX + ZMAX + 2];
+};
+
+// Deposit the low bits of v into the listed bit positions.
+__device__ __forceinline__ int64_t deposit(int64_t v, const uint8_t* bits, int nb) {
+  int64_t x = 0;
+  for (int i = 0; i < nb; ++i)
+    if ((v >> i) & 1) x |= (int64_t)1 << bits[i];
+  return x;
+}
+
+// Common per-CTA setup: gate coefficients, element offsets, outside bits.
+// Also builds the diagonal phase table (Z rotations * scale) and the
+// integer-cost phase table when requested.
+template <bool BWD>
+__device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShared& S, double2* ztab, double2* ctab) {
+  const int tid = threadIdx.x;
+  const int t = d.t, n = d.n;
+  if (tid < d.nxy) {
+    int f;
+    double k;
+    S.u[tid] = rot_form(angle_of(d.xy[tid].a, params), &f, &k);
+    S.form[tid] = f;
+  }
+  if (t > 8) {
+    for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
+  } else if (tid == 0) {
+    S.offhi[0] = 0;
+  }
+  if (tid == 0) {
+    // bits not in the tile, ascending
+    int j = 0, o = 0;
+    for (int b = 0; b < n; ++b) {
+      if (j < t && d.bits[j] == b)
+        ++j;
+      else
+        S.outside[o++] = (uint8_t)b;
+    }
+  }
+  if (!BWD && d.start == START_MCCLEAN && tid == 0) {
+    // Ry(pi/4)|0> = cos(pi/8)|0> + sin(pi/8)|1> on every qubit
+    double s8, c8;
+    sincospi(0.125, &s8, &c8);
+    double p = 1.0;
+    for (int k = 0; k < n; ++k) p *= c8;
+    S.startP[0] = p;
+    for (int k = 1; k <= n; ++k) {
+      double q = 1.0;
+      for (int i = 0; i < n - k; ++i) q *= c8;
+      for (int i = 0; i < k; ++i) q *= s8;
+      S.startP[k] = q;
+    }
+  }
+  if (d.has_diag) {
+    // scale K = prod kappa over the layer's X/Y rotations
+    double K = 1.0;
+    for (int i = 0; i < d.nscale; ++i) {
+      int f;
+      double k;
+      rot_form(angle_of(d.scale[i], params), &f, &k);
+      K *= k;
+    }
+    const int nz = d.nz;
+    for (int pat = tid; pat < (1 << nz); pat += NTHREADS) {
+      double2 ph = make_double2(K, 0.0);
+      for (int j = 0; j < nz; ++j) {
+        double s, c;
+        sincos(0.5 * angle_of(d.z[j].a, params), &s, &c);
+        // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170)
+        const double2 e = make_double2(c, ((pat >> j) & 1) ? s : -s);
+        ph = cmul<double2>(ph, e);
+      }
+      if (BWD) ph.y = -ph.y;
+      ztab[pat] = ph;
+    }
+  }
+  if (d.cost == COST_INT) {
+    const double g = angle_of(d.cost_angle, params) * d.cost_w0;
+    const int M = d.cost_maxabs;
+    for (int i = tid; i <= 2 * M; i += NTHREADS) {
+      double s, c;
+      sincos(g * (double)(i - M), &s, &c);
+      ctab[i] = make_double2(c, BWD ? s : -s);  // exp(-i gamma C) forward
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int zpattern(uint64_t x, const SweepDesc& d) {
+  int pat = 0;
+  for (int j = 0; j < d.nz; ++j) pat |= (int)((x >> d.z[j].gbit) & 1) << j;
+  return pat;
+}
+
+// ------------------------------------------------------------ forward sweep
+
+template <typename R>
+__global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_constant__ SweepDesc d, SweepPtrs<R> p) {
+  using C = typename C2T<R>::T;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ SetupShared S;
+  const int t = d.t, n = d.n;
+  const int tsize = 1 << t;
+  C* tile = (C*)smem;
+  double2* ztab = (double2*)(tile + tsize);
+  double2* ctab = ztab + (1 << d.nz);
+  sweep_setup<false>(d, p.params, S, ztab, ctab);
+
+  const int tid = threadIdx.x;
+  const LadderMasks lm = ladder_masks(n);
+  const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
+  const bool active = tid < tsize;
+  const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int64_t ntiles = (int64_t)1 << (n - t);
+  const double plus = exp2(-0.5 * n);
+  const bool diag_folded = d.cost == COST_INT && d.has_diag && d.nz == 0;
+  const double kfold = diag_folded ? ztab[0].x : 1.0;
+
+  for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
+    const int64_t base = deposit(tileid, S.outside, n - t);
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        uint64_t src = x;
+        if (d.pre == ENT_CNOT) src = ladder_inv(x, lm);
+        C v;
+        if (d.start == START_LOAD) {
+          v = p.psi_in[src];
+        } else if (d.start == START_MCCLEAN) {
+          v.x = (R)S.startP[__popcll(src)];
+          v.y = (R)0;
+        } else {
+          v.x = (R)plus;
+          v.y = (R)0;
+        }
+        if (d.pre == ENT_CZ && cz_negative(x)) v = cneg(v);
+        if (d.cost == COST_INT) {
+          double2 ph = ctab[p.cost_i[x] + d.cost_maxabs];
+          if (diag_folded) ph = make_double2(ph.x * kfold, ph.y * kfold);
+          v = cmul<C>(v, ph);
+        } else if (d.cost == COST_REAL) {
+          double s, c;
+          sincos(angle_of(d.cost_angle, p.params) * p.cost_d[x], &s, &c);
+          v = cmul<C>(v, make_double2(c, -s));
+        }
+        if (d.has_diag && !diag_folded) {
+          if (d.nz)
+            v = cmul<C>(v, ztab[zpattern(x, d)]);
+          else
+            v = cscale<C>(v, ztab[0].x);
+        }
+        tile[sw<R>(e)] = v;
+      }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int g = 0; g < d.nxy; ++g) {
+      const int j = d.xy[g].lbit, axis = d.xy[g].axis, form = S.form[g];
+      const R u = (R)S.u[g];
+      for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
+        const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
+        C a = tile[ia], b = tile[ib];
+        rot_pair<C, R>(a, b, axis, form, u, (R)1);
+        tile[ia] = a;
+        tile[ib] = b;
+      }
+      __syncthreads();
+    }
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        C v;
+        if (d.post == ENT_CNOT) {
+          // (E v)[y] = v[A^{-1} y]; the tile is a contiguous aligned block
+          v = tile[sw<R>((int)(ladder_inv(x, lm) & (uint64_t)(tsize - 1)))];
+        } else {
+          v = tile[sw<R>(e)];
+        }
+        if (d.post == ENT_CZ && cz_negative(x)) v = cneg(v);
+        p.psi_out[x] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ backward sweep
+//
+// Loads lambda and psi at the point after the sweep's gates, accumulates
+// Im<lam|P_q|psi> for every rotation of the sweep (the adjoint gradient,
+// mc_clean.py:68-77: -2 Re<psi|(-i P/2) lam> = Im<lam|P|psi>), then applies
+// the inverse gates to lambda (and to psi when it is uncomputed rather than
+// read from the stored history).
+
+template <typename R, bool UNCOMPUTE>
+__global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_constant__ SweepDesc d, SweepPtrs<R> p) {
+  using C = typename C2T<R>::T;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ SetupShared S;
+  const int t = d.t, n = d.n;
+  const int tsize = 1 << t;
+  C* tl = (C*)smem;
+  C* tp = tl + tsize;
+  double2* ztab = (double2*)(tp + tsize);
+  double2* ctab = ztab + (1 << d.nz);
+  sweep_setup<true>(d, p.params, S, ztab, ctab);
+
+  const int tid = threadIdx.x;
+  const LadderMasks lm = ladder_masks(n);
+  const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
+  const bool active = tid < tsize;
+  const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int64_t ntiles = (int64_t)1 << (n - t);
+  const bool diag_folded = d.cost == COST_INT && d.has_diag && d.nz == 0;
+  const double kfold = diag_folded ? ztab[0].x : 1.0;
+  const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
+
+  double acc_xy[TMAX], acc_z[ZMAX], acc_g = 0.0;
+#pragma unroll
+  for (int i = 0; i < TMAX; ++i) acc_xy[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < ZMAX; ++i) acc_z[i] = 0.0;
+
+  for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
+    const int64_t base = deposit(tileid, S.outside, n - t);
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        uint64_t src = x;
+        if (d.post == ENT_CNOT) src = ladder_fwd(x, lm);  // (E^{-1} v)[y] = v[A y]
+        C l = p.lam_in[src], q = p.psi_in[src];
+        if (d.post == ENT_CZ && cz_negative(x)) {
+          l = cneg(l);
+          q = cneg(q);
+        }
+        const double w = (double)l.x * (double)q.y - (double)l.y * (double)q.x;  // Im(conj(l) q)
+        if (d.gslot >= 0) {
+          const double cx = d.cost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x];
+          acc_g = fma(cx, w, acc_g);
+        }
+#pragma unroll
+        for (int j = 0; j < ZMAX; ++j)
+          if (j < d.nz) acc_z[j] += ((x >> d.z[j].gbit) & 1) ? -w : w;
+        tl[sw<R>(e)] = l;
+        tp[sw<R>(e)] = q;
+      }
+    }
+    __syncthreads();
+    // gradient reductions for the X/Y rotations (read-only pass)
+#pragma unroll
+    for (int g = 0; g < TMAX; ++g) {
+      if (g < d.nxy) {
+        const int j = d.xy[g].lbit;
+        const bool isx = d.xy[g].axis == AX_X;
+        double a = 0.0;
+        for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
+          const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
+          const C la = tl[ia], lb = tl[ib], qa = tp[ia], qb = tp[ib];
+          if (isx) {
+            // Im(conj(la) qb) + Im(conj(lb) qa)
+            a = fma((double)la.x, (double)qb.y, a);
+            a = fma(-(double)la.y, (double)qb.x, a);
+            a = fma((double)lb.x, (double)qa.y, a);
+            a = fma(-(double)lb.y, (double)qa.x, a);
+          } else {
+            // Y: -Re(conj(la) qb) + Re(conj(lb) qa)
+            a = fma(-(double)la.x, (double)qb.x, a);
+            a = fma(-(double)la.y, (double)qb.y, a);
+            a = fma((double)lb.x, (double)qa.x, a);
+            a = fma((double)lb.y, (double)qa.y, a);
+          }
+        }
+        acc_xy[g] += a;
+      }
+    }
+    __syncthreads();
+    // inverse rotations
+#pragma unroll 1
+    for (int g = d.nxy - 1; g >= 0; --g) {
+      const int j = d.xy[g].lbit, axis = d.xy[g].axis, form = S.form[g];
+      const R u = (R)S.u[g];
+      for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
+        const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
+        C a = tl[ia], b = tl[ib];
+        rot_pair<C, R>(a, b, axis, form, u, (R)-1);
+        tl[ia] = a;
+        tl[ib] = b;
+        if (UNCOMPUTE) {
+          C a2 = tp[ia], b2 = tp[ib];
+          rot_pair<C, R>(a2, b2, axis, form, u, (R)-1);
+          tp[ia] = a2;
+          tp[ib] = b2;
+        }
+      }
+      __syncthreads();
+    }
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        // position z in the after-pre index space that lands at x after pre^{-1}
+        uint64_t z = x;
+        if (d.pre == ENT_CNOT) z = ladder_fwd(x, lm);
+        const int le = d.pre == ENT_CNOT ? (int)(z & (uint64_t)(tsize - 1)) : e;
+        C l = tl[sw<R>(le)];
+        C q;
+        if (UNCOMPUTE) q = tp[sw<R>(le)];
+        // inverse diagonal and inverse cost phase at index z
+        if (d.has_diag && !diag_folded) {
+          if (d.nz) {
+            const double2 ph = ztab[zpattern(z, d)];
+            l = cmul<C>(l, ph);
+            if (UNCOMPUTE) q = cmul<C>(q, ph);
+          } else {
+            l = cscale<C>(l, ztab[0].x);
+            if (UNCOMPUTE) q = cscale<C>(q, ztab[0].x);
+          }
+        }
+        if (d.cost == COST_INT) {
+          double2 ph = ctab[p.cost_i[z] + d.cost_maxabs];
+          if (diag_folded) ph = make_double2(ph.x * kfold, ph.y * kfold);
+          l = cmul<C>(l, ph);
+          if (UNCOMPUTE) q = cmul<C>(q, ph);
+        } else if (d.cost == COST_REAL) {
+          double s, c;
+          sincos(gamma * p.cost_d[z], &s, &c);
+          l = cmul<C>(l, make_double2(c, s));
+          if (UNCOMPUTE) q = cmul<C>(q, make_double2(c, s));
+        }
+        if (d.pre == ENT_CZ && cz_negative(x)) {
+          l = cneg(l);
+          if (UNCOMPUTE) q = cneg(q);
+        }
+        p.lam_out[x] = l;
+        if (UNCOMPUTE) p.psi_out[x] = q;
+      }
+    }
+    __syncthreads();
+  }
+
+  // block reduction of the gradient accumulators -> partials[slot][blockIdx]
+  const int warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+  for (int g = 0; g < TMAX; ++g) {
+    if (g < d.nxy) {
+      const double v = warp_sum(acc_xy[g]);
+      if (lane == 0) S.red[warp][g] = v;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ZMAX; ++j) {
+    if (j < d.nz) {
+      const double v = warp_sum(acc_z[j]);
+      if (lane == 0) S.red[warp][TMAX + j] = v;
+    }
+  }
+  if (d.gslot >= 0) {
+    const double v = warp_sum(acc_g);
+    if (lane == 0) S.red[warp][TMAX + ZMAX] = v;
+  }
+  __syncthreads();
+  if (tid < TMAX + ZMAX + 1) {
+    int slot = -1;
+    if (tid < TMAX) {
+      if (tid < d.nxy) slot = d.xy[tid].slot;
+    } else if (tid < TMAX + ZMAX) {
+      if (tid - TMAX < d.nz) slot = d.z[tid - TMAX].slot;
+    } else {
+      slot = d.gslot;
+    }
+    if (slot >= 0) {
+      double s = 0.0;
+      for (int w = 0; w < NTHREADS / 32; ++w) s += S.red[w][tid];
+      p.partials[(int64_t)slot * p.G + blockIdx.x] = s;
+    }
+  }
+}
+
+// ------------------------------------------------------------ observable
+//
+// lam = O psi for O = sum of weighted Pauli terms (observable.py:45-73), and
+// the partial sums of Re<psi|lam> (base.py:17-20).  X/Y terms need the
+// partner amplitude and are taken from the staged tile.
+
+template <typename R>
+__global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_constant__ ObsDesc d, const typename C2T<R>::T* psi,
+                                                              typename C2T<R>::T* lam, const int32_t* cost_i,
+                                                              const double* cost_d, double* partials, int G) {
+  using C = typename C2T<R>::T;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int64_t offhi[32];
+  __shared__ uint8_t outside[QMAX];
+  __shared__ double red[NTHREADS / 32];
+  const int t = d.t, n = d.n;
+  const int tsize = 1 << t;
+  C* tile = (C*)smem;
+  const int tid = threadIdx.x;
+  if (t > 8) {
+    for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) offhi[k] = deposit((int64_t)k << 8, d.bits, t);
+  } else if (tid == 0) {
+    offhi[0] = 0;
+  }
+  if (tid == 0) {
+    int j = 0, o = 0;
+    for (int b = 0; b < n; ++b) {
+      if (j < t && d.bits[j] == b)
+        ++j;
+      else
+        outside[o++] = (uint8_t)b;
+    }
+  }
+  __syncthreads();
+  const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
+  const bool active = tid < tsize;
+  const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int64_t ntiles = (int64_t)1 << (n - t);
+  double eacc = 0.0;
+  for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
+    const int64_t base = deposit(tileid, outside, n - t);
+    if (d.nxy > 0) {
+      if (active)
+        for (int k = 0; k < nk; ++k) tile[sw<R>(tid + k * NTHREADS)] = psi[base | dep_lo | offhi[k]];
+      __syncthreads();
+    }
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
+        const C v = d.nxy > 0 ? tile[sw<R>(e)] : psi[x];
+        double lx = 0.0, ly = 0.0;
+        if (d.cost == COST_INT || d.cost == COST_REAL || d.ndiag > 0) {
+          double dv = 0.0;
+          if (d.cost == COST_INT) {
+            dv = d.cost_w0 * (double)cost_i[x];
+          } else if (d.cost == COST_REAL) {
+            dv = cost_d[x];
+          } else {
+            int cnt = 0;
+            double wcur = d.term[0].w;
+            for (int i = 0; i < d.ndiag; ++i) {
+              const ObsTerm& tm = d.term[i];
+              if (tm.w != wcur) {
+                dv = fma(wcur, (double)cnt, dv);
+                cnt = 0;
+                wcur = tm.w;
+              }
+              int s = (int)((x >> tm.b0) & 1);
+              if (tm.kind == 3) s ^= (int)((x >> tm.b1) & 1);
+              cnt += 1 - 2 * s;
+            }
+            dv = fma(wcur, (double)cnt, dv);
+          }
+          lx = dv * (double)v.x;
+          ly = dv * (double)v.y;
+        }
+        for (int i = d.ndiag; i < d.ndiag + d.nxy; ++i) {
+          const ObsTerm& tm = d.term[i];
+          const C u = tile[sw<R>(e ^ (1 << tm.lb0))];
+          if (tm.kind == 0) {
+            lx = fma(tm.w, (double)u.x, lx);
+            ly = fma(tm.w, (double)u.y, ly);
+          } else {
+            // (Y psi)_x = -i psi_partner (bit 0) or +i psi_partner (bit 1)
+            const double sgn = ((x >> tm.b0) & 1) ? 1.0 : -1.0;
+            lx = fma(-sgn * tm.w, (double)u.y, lx);
+            ly = fma(sgn * tm.w, (double)u.x, ly);
+          }
+        }
+        eacc = fma((double)v.x, lx, fma((double)v.y, ly, eacc));
+        if (d.store) {
+          C o;
+          if (d.accumulate) {
+            o = lam[x];
+            o.x = (R)((double)o.x + lx);
+            o.y = (R)((double)o.y + ly);
+          } else {
+            o.x = (R)lx;
+            o.y = (R)ly;
+          }
+          lam[x] = o;
+        }
+      }
+    }
+    if (d.nxy > 0) __syncthreads();
+  }
+  const double v = warp_sum(eacc);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NTHREADS / 32; ++w) s += red[w];
+    partials[(int64_t)d.eslot * G + blockIdx.x] = s;
+  }
+}
+
+// ------------------------------------------------------------ gamma at the start
+//
+// QAOA: the gamma_0 reduction sits at the start state, which no backward
+// sweep loads.  One pass over (lambda, psi_0).
+template <typename R>
+__global__ void __launch_bounds__(NTHREADS) cost_reduce_kernel(int n, const typename C2T<R>::T* lam,
+                                                               const typename C2T<R>::T* psi, int start_plus,
+                                                               int cost, double w0, const int32_t* cost_i,
+                                                               const double* cost_d, double* partials, int slot,
+                                                               int G) {
+  __shared__ double red[NTHREADS / 32];
+  const int64_t N = (int64_t)1 << n;
+  const double plus = exp2(-0.5 * n);
+  double acc = 0.0;
+  for (int64_t x = (int64_t)blockIdx.x * NTHREADS + threadIdx.x; x < N; x += (int64_t)gridDim.x * NTHREADS) {
+    const auto l = lam[x];
+    double qx, qy;
+    if (start_plus) {
+      qx = plus;
+      qy = 0.0;
+    } else {
+      qx = (double)psi[x].x;
+      qy = (double)psi[x].y;
+    }
+    const double w = (double)l.x * qy - (double)l.y * qx;
+    const double cx = cost == COST_INT ? w0 * (double)cost_i[x] : cost_d[x];
+    acc = fma(cx, w, acc);
+  }
+  const double v = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NTHREADS / 32; ++w) s += red[w];
+    partials[(int64_t)slot * G + blockIdx.x] = s;
+  }
+}
+
+// ------------------------------------------------------------ finaliser
+//
+// grad[p] = factor(p) * sum over the parameter's slots and CTAs, in a fixed
+// order (deterministic).  Layout kinds:
+//   0 McClean: parameter p <-> slot p
+//   1 QAOA:    layer i: beta slots i*(n+1) + q (q < n), gamma slot i*(n+1) + n
+//              (factor 2); grad layout [p, 2] with column 0 beta, 1 gamma.
+__global__ void finalize_kernel(const double* partials, int G, int kind, int n, int nparam, int eslot, int neslots,
+                                double* expec, double* grad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && expec) {
+    double e = 0.0;
+    for (int s = 0; s < neslots; ++s)
+      for (int b = 0; b < G; ++b) e += partials[(int64_t)(eslot + s) * G + b];
+    *expec = e;
+  }
+  if (i >= nparam || !grad) return;
+  double g = 0.0;
+  if (kind == 0) {
+    for (int b = 0; b < G; ++b) g += partials[(int64_t)i * G + b];
+  } else {
+    const int layer = i >> 1;
+    if ((i & 1) == 0) {
+      for (int q = 0; q < n; ++q)
+        for (int b = 0; b < G; ++b) g += partials[(int64_t)(layer * (n + 1) + q) * G + b];
+    } else {
+      for (int b = 0; b < G; ++b) g += partials[(int64_t)(layer * (n + 1) + n) * G + b];
+      g *= 2.0;
+    }
+  }
+  grad[i] = g;
+}
+
+// ------------------------------------------------------------ launchers
+
+template <typename R>
+static size_t sweep_smem(const SweepDesc& d, bool bwd) {
+  using C = typename C2T<R>::T;
+  size_t s = (size_t)(bwd ? 2 : 1) * ((size_t)1 << d.t) * sizeof(C);
+  s += ((size_t)1 << d.nz) * sizeof(double2);
+  if (d.cost == COST_INT) s += (size_t)(2 * d.cost_maxabs + 1) * sizeof(double2);
+  return s;
+}
+
+template <typename R>
+cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st) {
+  const size_t smem = sweep_smem<R>(d, false);
+  cudaError_t e = cudaFuncSetAttribute(sweep_fwd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  sweep_fwd_kernel<R><<<grid, NTHREADS, smem, st>>>(d, p);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st) {
+  const size_t smem = sweep_smem<R>(d, true);
+  cudaError_t e;
+  if (uncompute) {
+    e = cudaFuncSetAttribute(sweep_bwd_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    sweep_bwd_kernel<R, true><<<grid, NTHREADS, smem, st>>>(d, p);
+  } else {
+    e = cudaFuncSetAttribute(sweep_bwd_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    sweep_bwd_kernel<R, false><<<grid, NTHREADS, smem, st>>>(d, p);
+  }
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_observable(const ObsDesc& d, const typename C2T<R>::T* psi, typename C2T<R>::T* lam,
+                              const int32_t* cost_i, const double* cost_d, double* partials, int G, int grid,
+                              cudaStream_t st) {
+  using C = typename C2T<R>::T;
+  const size_t smem = d.nxy > 0 ? ((size_t)1 << d.t) * sizeof(C) : 0;
+  cudaError_t e = cudaFuncSetAttribute(observable_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  observable_kernel<R><<<grid, NTHREADS, smem, st>>>(d, psi, lam, cost_i, cost_d, partials, G);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_cost_reduce(int n, const typename C2T<R>::T* lam, const typename C2T<R>::T* psi, int start_plus,
+                               int cost, double w0, const int32_t* cost_i, const double* cost_d, double* partials,
+                               int slot, int G, cudaStream_t st) {
+  cost_reduce_kernel<R><<<G, NTHREADS, 0, st>>>(n, lam, psi, start_plus, cost, w0, cost_i, cost_d, partials, slot, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const double* partials, int G, int kind, int n, int nparam, int eslot, int neslots,
+                            double* expec, double* grad, cudaStream_t st) {
+  const int threads = 128;
+  const int blocks = nparam > 0 ? (nparam + threads - 1) / threads : 1;
+  finalize_kernel<<<blocks, threads, 0, st>>>(partials, G, kind, n, nparam, eslot, neslots, expec, grad);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_sweep_fwd<double>(const SweepDesc&, const SweepPtrs<double>&, int, cudaStream_t);
+template cudaError_t launch_sweep_fwd<float>(const SweepDesc&, const SweepPtrs<float>&, int, cudaStream_t);
+template cudaError_t launch_sweep_bwd<double>(const SweepDesc&, const SweepPtrs<double>&, bool, int, cudaStream_t);
+template cudaError_t launch_sweep_bwd<float>(const SweepDesc&, const SweepPtrs<float>&, bool, int, cudaStream_t);
+template cudaError_t launch_observable<double>(const ObsDesc&, const double2*, double2*, const int32_t*, const double*,
+                                               double*, int, int, cudaStream_t);
+template cudaError_t launch_observable<float>(const ObsDesc&, const float2*, float2*, const int32_t*, const double*,
+                                              double*, int, int, cudaStream_t);
+template cudaError_t launch_cost_reduce<double>(int, const double2*, const double2*, int, int, double, const int32_t*,
+                                                const double*, double*, int, int, cudaStream_t);
+template cudaError_t launch_cost_reduce<float>(int, const float2*, const float2*, int, int, double, const int32_t*,
+                                               const double*, double*, int, int, cudaStream_t);
+
+}  // namespace qg

@@ -1,0 +1,108 @@
+"""The C-ABI library builds, loads and exports every symbol include/qgrad.h
+declares; host-only entry points validate their arguments (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "qgrad.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(qg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    names = _declared()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, name
+
+
+def test_status_strings_and_version():
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.qg_version() >= 1
+    assert lib.qg_status_string(0) == b"ok"
+    assert lib.qg_status_string(3) == b"workspace too small"
+
+
+def _create(n, L, axes, kind=(3,), q0=(0,), q1=(1,), w=(1.0,), ent=1, place=0):
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    ax = np.ascontiguousarray(axes, dtype=np.int32)
+    k = np.array(kind, np.int32)
+    a = np.array(q0, np.int32)
+    b = np.array(q1, np.int32)
+    ww = np.array(w, np.float64)
+    h = ctypes.c_void_p()
+    st = lib.qg_mcclean_create(n, L, ax.ctypes.data_as(ctypes.c_void_p), ent, place, len(k),
+                               k.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p),
+                               b.ctypes.data_as(ctypes.c_void_p), ww.ctypes.data_as(ctypes.c_void_p),
+                               ctypes.byref(h))
+    return st, h
+
+
+def test_create_validates_like_the_reference():
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    st, h = _create(4, 2, np.zeros((2, 4)))
+    assert st == 0 and h.value
+    nparams = ctypes.c_int()
+    assert lib.qg_num_params(h, ctypes.byref(nparams)) == 0 and nparams.value == 8
+    for op in (0, 1, 2):
+        b = ctypes.c_size_t()
+        assert lib.qg_workspace_size(h, 0, op, ctypes.byref(b)) == 0 and b.value > 0
+    lib.qg_destroy(h)
+    # invalid axis -> QG_ERR_INVALID (mc_clean.py:391-392 raises ValueError)
+    st, h = _create(4, 1, [[0, 1, 3, 0]])
+    assert st == _lib.QG_ERR_INVALID and b"Invalid axis" in lib.qg_last_error()
+    # zz in the lower triangle -> invalid (observable.py:57-64)
+    st, h = _create(4, 1, [[0, 0, 0, 0]], q0=(2,), q1=(1,))
+    assert st == _lib.QG_ERR_INVALID
+    with pytest.raises(ValueError):
+        _lib.check(st)
+    # too many qubits -> unsupported
+    st, h = _create(40, 0, np.zeros((0, 40)))
+    assert st == _lib.QG_ERR_UNSUPPORTED
+
+
+def test_history_needs_more_workspace_than_uncompute():
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    st, h = _create(20, 10, np.zeros((10, 20)))
+    assert st == 0
+    sizes = []
+    for op in (0, 1, 2):
+        b = ctypes.c_size_t()
+        lib.qg_workspace_size(h, 0, op, ctypes.byref(b))
+        sizes.append(b.value)
+    lib.qg_destroy(h)
+    S = 16 * 2 ** 20
+    assert sizes[0] >= S and sizes[2] >= 2 * S and sizes[1] > sizes[2]
+
+
+def test_product_path_fails_loudly_without_gpu():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("has a GPU")
+    from qradient_gb300 import McClean
+
+    zz = np.full((3, 3), None)
+    zz[0, 1] = 1.0
+    c = McClean(3, {"zz": zz}, 1)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        c.grad_run()
