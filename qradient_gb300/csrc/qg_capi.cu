@@ -166,8 +166,7 @@ struct LayerGate {
   int slot;
 };
 
-int build_layer(int n, const Layout& lay, const std::vector<LayerGate>& g, int ent, int placement,
-                std::vector<SweepDesc>& out) {
+int build_layer(int n, const Layout& lay, const std::vector<LayerGate>& g, int8_t pre, std::vector<SweepDesc>& out) {
   const int ns = (int)lay.tiles.size();
   std::vector<SweepDesc> sw;
   for (int s = 0; s < ns; ++s) sw.push_back(blank_sweep(n, lay.tiles[s]));
@@ -207,28 +206,16 @@ int build_layer(int n, const Layout& lay, const std::vector<LayerGate>& g, int e
     z.a = g[q].a;
     d.has_diag = 1;
   }
-  if (ent != QG_ENT_NONE) {
-    const int8_t e = ent == QG_ENT_CNOT_LADDER ? ENT_CNOT : ENT_CZ;
-    if (placement == QG_PLACE_BEFORE)
-      sw[0].pre = e;
-    else
-      sw[0].post = e;
-  }
-  if (placement == QG_PLACE_BEFORE || ent == QG_ENT_NONE) {
-    for (auto& d : sw) out.push_back(d);
-    for (auto& d : extra) out.push_back(d);
-  } else {
-    // rotations commute, so run the B sweeps first and finish with A + entangler
-    for (int s = 1; s < ns; ++s) out.push_back(sw[s]);
-    for (auto& d : extra) out.push_back(d);
-    out.push_back(sw[0]);
-  }
+  sw[0].pre = pre;  // entangler preceding this layer's rotations, gathered on load
+  for (auto& d : sw) out.push_back(d);
+  for (auto& d : extra) out.push_back(d);
   return QG_OK;
 }
 
 struct Program {
   Layout lay;
   std::vector<SweepDesc> sweeps;
+  int8_t obs_pre = ENT_NONE;  // entangler between the last sweep and the observable
   int first_param = 0;   // first sweep with gradient slots
   int nslots = 0;        // gradient slots (before the expectation slots)
   int grad_kind = 0;     // finalize layout
@@ -247,16 +234,23 @@ int build_program(const qg_circuit* c, int dtype, bool with_ini, Program& P) {
       // Ry(pi/4) on every qubit of the caller's state (mc_clean.py:55-56)
       std::vector<LayerGate> g(n);
       for (int q = 0; q < n; ++q) g[q] = LayerGate{AX_Y, angle_fixed(0.78539816339744830962), -1};
-      int st = build_layer(n, P.lay, g, QG_ENT_NONE, QG_PLACE_BEFORE, P.sweeps);
+      int st = build_layer(n, P.lay, g, ENT_NONE, P.sweeps);
       if (st) return st;
     }
     P.first_param = (int)P.sweeps.size();
+    const int8_t e = c->entangler == QG_ENT_CNOT_LADDER ? ENT_CNOT
+                     : c->entangler == QG_ENT_CZ_LADDER ? ENT_CZ
+                                                        : ENT_NONE;
     for (int i = 0; i < c->L; ++i) {
       std::vector<LayerGate> g(n);
       for (int q = 0; q < n; ++q) g[q] = LayerGate{c->axes[i * n + q], angle_param(i * n + q), i * n + q};
-      int st = build_layer(n, P.lay, g, c->entangler, c->placement, P.sweeps);
+      // placement before: E R per layer (mc_clean.py:58-62); after: R E, i.e.
+      // E in front of every later layer and once more before the observable
+      const int8_t pre = c->placement == QG_PLACE_BEFORE ? e : (i > 0 ? e : ENT_NONE);
+      int st = build_layer(n, P.lay, g, pre, P.sweeps);
       if (st) return st;
     }
+    if (c->placement == QG_PLACE_AFTER && c->L > 0) P.obs_pre = e;
   } else {
     const int p = c->L;
     P.nparams = 2 * p;
@@ -267,7 +261,7 @@ int build_program(const qg_circuit* c, int dtype, bool with_ini, Program& P) {
       std::vector<LayerGate> g(n);
       for (int q = 0; q < n; ++q) g[q] = LayerGate{AX_X, angle_param(2 * i), i * (n + 1) + q};
       const size_t s0 = P.sweeps.size();
-      int st = build_layer(n, P.lay, g, QG_ENT_NONE, QG_PLACE_BEFORE, P.sweeps);
+      int st = build_layer(n, P.lay, g, ENT_NONE, P.sweeps);
       if (st) return st;
       SweepDesc& a = P.sweeps[s0];
       a.cost = (int8_t)c->cost_kind;
@@ -307,6 +301,8 @@ struct WsLayout {
   size_t partials = 0, lam = 0, psi = 0, cost = 0, total = 0;
   size_t state_bytes = 0;
   int nstates_psi = 0;
+  int nstates_lam = 0;
+  bool pingpong = false;  // a CNOT-ladder gather needs distinct in / out buffers
   int G = 1, grid_fwd = 1;
   int neslots = 1;
 };
@@ -339,15 +335,19 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
   w.grid_fwd = (int)std::min<int64_t>(ntiles, (int64_t)sms * std::max(per_sm, 2));
   w.neslots = obs_sweeps_needed(c, P.lay, op != QG_OP_RUN);
   const int m = (int)P.sweeps.size();
+  w.pingpong = P.obs_pre == ENT_CNOT;
+  for (const auto& d : P.sweeps) w.pingpong = w.pingpong || d.pre == ENT_CNOT;
+  const int two = w.pingpong ? 2 : 1;
   if (op == QG_OP_GRAD_HISTORY)
     w.nstates_psi = m;
   else
-    w.nstates_psi = 1;
+    w.nstates_psi = two;
+  w.nstates_lam = op == QG_OP_RUN ? 0 : two;
   size_t off = 0;
   w.partials = off;
   off += align_up((size_t)(P.nslots + w.neslots) * w.G * sizeof(double));
   w.lam = off;
-  off += align_up(op == QG_OP_RUN ? 0 : w.state_bytes);
+  off += align_up((size_t)w.nstates_lam * w.state_bytes);
   w.psi = off;
   off += align_up((size_t)w.nstates_psi * w.state_bytes);
   w.cost = off;
@@ -396,6 +396,7 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
     d->t = (int)lay.tiles[s].size();
     for (size_t i = 0; i < lay.tiles[s].size(); ++i) d->bits[i] = (uint8_t)lay.tiles[s][i];
     d->store = lam != nullptr;
+    d->pre = P.obs_pre;
   };
   if (c->kind == 1 && grad) {
     // lam = C psi with the classical cost (qaoa.py:56-57)
@@ -457,11 +458,20 @@ int forward(const qg_circuit* c, const Program& P, const WsLayout& W, const doub
   p.cost_d = (const double*)(ws + W.cost);
   p.partials = (double*)(ws + W.partials);
   p.G = W.G;
-  C* psi0 = (C*)(ws + W.psi);
+  const size_t N = (size_t)1 << c->n;
+  C* buf[2] = {(C*)(ws + W.psi), W.pingpong && !history ? (C*)(ws + W.psi) + N : nullptr};
+  int cur = 0;
   const int m = (int)P.sweeps.size();
   const C* in = (const C*)ini;
   for (int k = 0; k < m; ++k) {
-    C* out = history ? psi0 + (size_t)k * ((size_t)1 << c->n) : psi0;
+    C* out;
+    if (history) {
+      out = buf[0] + (size_t)k * N;
+    } else {
+      // in place, except that a ladder gather reads other tiles: write the other buffer
+      if (P.sweeps[k].pre == ENT_CNOT && in == buf[cur]) cur ^= 1;
+      out = buf[cur];
+    }
     p.psi_in = in;
     p.psi_out = out;
     QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd, st));
@@ -508,8 +518,12 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
   const C* fin = nullptr;
   s = forward<R>(c, P, W, params, ini, history, ws, st, &fin);
   if (s) return s;
-  C* lam = (C*)(ws + W.lam);
-  s = run_observable<R>(c, P, W, true, fin, lam, ws, st);
+  const size_t N = (size_t)1 << c->n;
+  C* lbuf[2] = {(C*)(ws + W.lam), W.pingpong ? (C*)(ws + W.lam) + N : nullptr};
+  C* pbuf[2] = {(C*)(ws + W.psi), W.pingpong && !history ? (C*)(ws + W.psi) + N : nullptr};
+  int lc = 0, pc = 0;
+  if (!history) pc = fin == pbuf[1] ? 1 : 0;
+  s = run_observable<R>(c, P, W, true, fin, lbuf[lc], ws, st);
   if (s) return s;
   SweepPtrs<R> p;
   memset(&p, 0, sizeof p);
@@ -518,25 +532,30 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
   p.cost_d = (const double*)(ws + W.cost);
   p.partials = (double*)(ws + W.partials);
   p.G = W.G;
-  p.lam_in = lam;
-  p.lam_out = lam;
   C* psi0 = (C*)(ws + W.psi);
   const int m = (int)P.sweeps.size();
   for (int k = m - 1; k >= P.first_param; --k) {
+    SweepDesc d = P.sweeps[k];
+    // undo, on load, the entangler the forward applied right after sweep k
+    d.lam_undo = k + 1 < m ? P.sweeps[k + 1].pre : P.obs_pre;
+    d.psi_undo = history ? ENT_NONE : (k + 1 < m ? P.sweeps[k + 1].pre : ENT_NONE);
+    p.lam_in = lbuf[lc];
+    if (d.lam_undo == ENT_CNOT) lc ^= 1;
+    p.lam_out = lbuf[lc];
     if (history) {
-      p.psi_in = psi0 + (size_t)k * ((size_t)1 << c->n);
+      p.psi_in = psi0 + (size_t)k * N;
       p.psi_out = nullptr;
     } else {
-      p.psi_in = psi0;
-      p.psi_out = psi0;
+      p.psi_in = pbuf[pc];
+      if (d.psi_undo == ENT_CNOT) pc ^= 1;
+      p.psi_out = pbuf[pc];
     }
-    QG_CUDA(launch_sweep_bwd<R>(P.sweeps[k], p, !history, W.G, st));
+    QG_CUDA(launch_sweep_bwd<R>(d, p, !history, W.G, st));
   }
+  C* lam = lbuf[lc];
   if (c->kind == 1 && c->L > 0) {
     // gamma_0 at the start state (qaoa.py:65-68 for i = 0)
-    const C* psi_start = (const C*)ini;
-    if (!history && ini == nullptr) psi_start = nullptr;
-    if (!history && ini != nullptr) psi_start = psi0;  // uncomputed back to the start
+    const C* psi_start = history ? (const C*)ini : (ini ? pbuf[pc] : nullptr);
     QG_CUDA(launch_cost_reduce<R>(c->n, lam, psi_start, psi_start == nullptr, c->cost_kind, c->cost_w0,
                                   p.cost_i, p.cost_d, p.partials, 0 * (c->n + 1) + c->n, W.G, st));
   }

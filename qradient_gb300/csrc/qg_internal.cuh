@@ -34,7 +34,9 @@ constexpr int MAX_COST_TAB = 4097; // entries of the integer cost-phase table
 
 enum Axis : int8_t { AX_X = 0, AX_Y = 1, AX_Z = 2 };
 
-// Entangler applied at a sweep's load (pre) or store (post).
+// Entangler.  The CNOT ladder permutes amplitudes across tiles, so it is
+// only ever applied as a gather while a sweep loads its input (from a buffer
+// other than the one it writes); the CZ ladder is a sign and works in place.
 enum Ent : int8_t {
   ENT_NONE = 0,
   ENT_CNOT = 1,  // reference CNOT ladder, state.py:209-251 (odd pairs, then even pairs)
@@ -86,11 +88,12 @@ struct SweepDesc {
   AngleRef scale[QMAX];
   uint8_t bits[TMAX];      // global bit positions of the tile bits, ascending
   int8_t has_diag;         // apply the diagonal (phase table * scale) in this sweep
-  int8_t pre;              // Ent applied to the input before the gates
-  int8_t post;             // Ent applied after the gates
+  int8_t pre;              // forward: Ent applied to the input as it is loaded (before the gates)
+  int8_t lam_undo;         // backward: Ent undone on lambda as it is loaded
   int8_t start;            // Start kind of the forward input
   int8_t cost;             // CostKind: QAOA exp(-i gamma C), applied before the gates
-  int8_t pad[3];
+  int8_t psi_undo;         // backward: Ent undone on psi as it is loaded (uncompute mode)
+  int8_t pad[2];
   AngleRef cost_angle;     // gamma
   int32_t cost_maxabs;     // |m| <= cost_maxabs (COST_INT)
   int32_t gslot;           // backward: slot of Im<lam|C|psi> at the load point, -1 if none
@@ -116,6 +119,8 @@ struct ObsDesc {
   int8_t accumulate;   // 0: lam = O_part psi; 1: lam += O_part psi
   int8_t store;        // write lam
   int8_t cost;         // diagonal from the QAOA cost (CostKind) instead of the diagonal terms
+  int8_t pre;          // Ent applied to psi as it is loaded (entangler after the last layer)
+  int8_t pad0[3];
   int32_t ndiag;       // diagonal terms (first)
   int32_t nxy;         // X/Y terms handled here (after the diagonal ones)
   int32_t eslot;       // slot of the expectation partial sums

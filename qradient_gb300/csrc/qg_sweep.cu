@@ -102,6 +102,14 @@ __device__ __forceinline__ C cneg(C a) {
   return a;
 }
 
+// (E psi)[x] for the entangler E: a gather for the CNOT ladder, a sign for CZ.
+template <typename C>
+__device__ __forceinline__ C load_pre(const C* psi, uint64_t x, int ent, const LadderMasks& lm) {
+  C v = psi[ent == ENT_CNOT ? ladder_inv(x, lm) : x];
+  if (ent == ENT_CZ && cz_negative(x)) v = cneg(v);
+  return v;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -341,15 +349,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        C v;
-        if (d.post == ENT_CNOT) {
-          // (E v)[y] = v[A^{-1} y]; the tile is a contiguous aligned block
-          v = tile[sw<R>((int)(ladder_inv(x, lm) & (uint64_t)(tsize - 1)))];
-        } else {
-          v = tile[sw<R>(e)];
-        }
-        if (d.post == ENT_CZ && cz_negative(x)) v = cneg(v);
-        p.psi_out[x] = v;
+        p.psi_out[x] = tile[sw<R>(e)];
       }
     }
     __syncthreads();
@@ -399,13 +399,11 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        uint64_t src = x;
-        if (d.post == ENT_CNOT) src = ladder_fwd(x, lm);  // (E^{-1} v)[y] = v[A y]
-        C l = p.lam_in[src], q = p.psi_in[src];
-        if (d.post == ENT_CZ && cz_negative(x)) {
-          l = cneg(l);
-          q = cneg(q);
-        }
+        // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y]
+        C l = p.lam_in[d.lam_undo == ENT_CNOT ? ladder_fwd(x, lm) : x];
+        C q = p.psi_in[d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x];
+        if (d.lam_undo == ENT_CZ && cz_negative(x)) l = cneg(l);
+        if (d.psi_undo == ENT_CZ && cz_negative(x)) q = cneg(q);
         const double w = (double)l.x * (double)q.y - (double)l.y * (double)q.x;  // Im(conj(l) q)
         if (d.gslot >= 0) {
           const double cx = d.cost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x];
@@ -471,13 +469,10 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        // position z in the after-pre index space that lands at x after pre^{-1}
-        uint64_t z = x;
-        if (d.pre == ENT_CNOT) z = ladder_fwd(x, lm);
-        const int le = d.pre == ENT_CNOT ? (int)(z & (uint64_t)(tsize - 1)) : e;
-        C l = tl[sw<R>(le)];
+        const uint64_t z = x;
+        C l = tl[sw<R>(e)];
         C q;
-        if (UNCOMPUTE) q = tp[sw<R>(le)];
+        if (UNCOMPUTE) q = tp[sw<R>(e)];
         // inverse diagonal and inverse cost phase at index z
         if (d.has_diag && !diag_folded) {
           if (d.nz) {
@@ -499,10 +494,6 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
           sincos(gamma * p.cost_d[z], &s, &c);
           l = cmul<C>(l, make_double2(c, s));
           if (UNCOMPUTE) q = cmul<C>(q, make_double2(c, s));
-        }
-        if (d.pre == ENT_CZ && cz_negative(x)) {
-          l = cneg(l);
-          if (UNCOMPUTE) q = cneg(q);
         }
         p.lam_out[x] = l;
         if (UNCOMPUTE) p.psi_out[x] = q;
@@ -587,19 +578,23 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int64_t ntiles = (int64_t)1 << (n - t);
+  const LadderMasks lm = ladder_masks(n);
   double eacc = 0.0;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, outside, n - t);
     if (d.nxy > 0) {
       if (active)
-        for (int k = 0; k < nk; ++k) tile[sw<R>(tid + k * NTHREADS)] = psi[base | dep_lo | offhi[k]];
+        for (int k = 0; k < nk; ++k) {
+          const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
+          tile[sw<R>(tid + k * NTHREADS)] = load_pre<C>(psi, x, d.pre, lm);
+        }
       __syncthreads();
     }
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
-        const C v = d.nxy > 0 ? tile[sw<R>(e)] : psi[x];
+        const C v = d.nxy > 0 ? tile[sw<R>(e)] : load_pre<C>(psi, x, d.pre, lm);
         double lx = 0.0, ly = 0.0;
         if (d.cost == COST_INT || d.cost == COST_REAL || d.ndiag > 0) {
           double dv = 0.0;
