@@ -270,7 +270,12 @@ int build_program(const qg_circuit* c, int dtype, bool with_ini, Program& P) {
       a.cost_w0 = c->cost_w0;
       // gamma_{i+1} reduction at the end of layer i (qaoa.py:65-68, moved to
       // the equivalent point before the cost phase of layer i+1)
-      if (i + 1 < p) P.sweeps.back().gslot = (i + 1) * (n + 1) + n;
+      if (i + 1 < p) {
+        SweepDesc& last = P.sweeps.back();
+        last.gslot = (i + 1) * (n + 1) + n;
+        last.gcost = (int8_t)c->cost_kind;
+        last.cost_w0 = c->cost_w0;
+      }
     }
   }
   if (P.sweeps.empty()) {

@@ -93,7 +93,8 @@ struct SweepDesc {
   int8_t start;            // Start kind of the forward input
   int8_t cost;             // CostKind: QAOA exp(-i gamma C), applied before the gates
   int8_t psi_undo;         // backward: Ent undone on psi as it is loaded (uncompute mode)
-  int8_t pad[2];
+  int8_t gcost;            // CostKind of the gslot reduction
+  int8_t pad;
   AngleRef cost_angle;     // gamma
   int32_t cost_maxabs;     // |m| <= cost_maxabs (COST_INT)
   int32_t gslot;           // backward: slot of Im<lam|C|psi> at the load point, -1 if none

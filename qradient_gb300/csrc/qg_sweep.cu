@@ -172,6 +172,8 @@ __device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u, R 
 
 struct SetupShared {
   double u[TMAX];
+  double kappa[TMAX];
+  double K;        // product of the folded scale factors (diagonal sweeps)
   int form[TMAX];
   int64_t offhi[32];   // deposit(k << 8) for the element loop
   uint8_t outside[QMAX];
@@ -199,6 +201,7 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
     double k;
     S.u[tid] = rot_form(angle_of(d.xy[tid].a, params), &f, &k);
     S.form[tid] = f;
+    S.kappa[tid] = k;
   }
   if (t > 8) {
     for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
@@ -238,6 +241,7 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
       rot_form(angle_of(d.scale[i], params), &f, &k);
       K *= k;
     }
+    if (tid == 0) S.K = K;
     const int nz = d.nz;
     for (int pat = tid; pat < (1 << nz); pat += NTHREADS) {
       double2 ph = make_double2(K, 0.0);
@@ -386,6 +390,18 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   const bool diag_folded = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double kfold = diag_folded ? ztab[0].x : 1.0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
+  // Uncomputing psi: the scaled inverse rotations return psi / kappa per
+  // rotation, while the forward stored psi with the scale of the forward
+  // scaled forms.  Keeping <lam|P|psi> unscaled at every sweep boundary needs
+  // psi multiplied by (prod own kappa)^2 (/ K^2 on the diagonal sweep, where
+  // the diagonal already multiplies by K).
+  double psi_mult = 1.0;
+  if (UNCOMPUTE) {
+    double own = 1.0;
+    for (int g = 0; g < d.nxy; ++g) own *= S.kappa[g];
+    psi_mult = own * own;
+    if (d.has_diag) psi_mult /= S.K * S.K;
+  }
 
   double acc_xy[TMAX], acc_z[ZMAX], acc_g = 0.0;
 #pragma unroll
@@ -406,7 +422,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
         if (d.psi_undo == ENT_CZ && cz_negative(x)) q = cneg(q);
         const double w = (double)l.x * (double)q.y - (double)l.y * (double)q.x;  // Im(conj(l) q)
         if (d.gslot >= 0) {
-          const double cx = d.cost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x];
+          const double cx = d.gcost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x];
           acc_g = fma(cx, w, acc_g);
         }
 #pragma unroll
@@ -496,7 +512,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
           if (UNCOMPUTE) q = cmul<C>(q, make_double2(c, s));
         }
         p.lam_out[x] = l;
-        if (UNCOMPUTE) p.psi_out[x] = q;
+        if (UNCOMPUTE) p.psi_out[x] = cscale<C>(q, psi_mult);
       }
     }
     __syncthreads();

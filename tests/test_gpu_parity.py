@@ -112,12 +112,14 @@ def test_mcclean_many_z_rotations():
     axes[0, 3] = 0
     rng = np.random.default_rng(11)
     angles = rng.uniform(0, 2 * np.pi, (L, n))
-    c = {"axes": axes, "angles": angles, "kind": np.array([3]), "q0": np.array([0]), "q1": np.array([1]),
-         "w": np.array([1.0])}
-    E0, g0 = O.mcclean_grad(n, axes, angles, O.Terms([3], [0], [1], [1.0]))
-    circ = _mcclean(n, L, c)
-    E, g = circ.grad_run()
-    assert abs(E - E0) <= TOL128 and rel_err(g, g0) <= TOL128
+    kind, q0, q1, w = [3, 0, 1], [0, 2, 5], [1, 2, 5], [1.0, 0.6, -0.8]
+    c = {"axes": axes, "angles": angles, "kind": np.array(kind), "q0": np.array(q0), "q1": np.array(q1),
+         "w": np.array(w)}
+    E0, g0 = O.mcclean_grad(n, axes, angles, O.Terms(kind, q0, q1, w))
+    for mode in ("history", "uncompute"):
+        circ = _mcclean(n, L, c, grad_mode=mode)
+        E, g = circ.grad_run()
+        assert abs(E - E0) <= TOL128 and rel_err(g, g0) <= TOL128, (mode, rel_err(g, g0))
 
 
 def test_mcclean_chain_n20_c128_and_c64(golden):
