@@ -1,0 +1,349 @@
+"""Benchmark of the McClean adjoint grad_run on GB300.
+
+Workload (the spec configuration): McClean n=24 qubits, L=50 layers,
+complex128, ZZ-chain observable sum_i Z_i Z_{i+1}, seeded random axes and
+angles (numpy default_rng(24)), the reference's CNOT-ladder-before-rotations
+layer.  A step is one full grad_run (E and all L*n gradients).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+value      circuits/s over the timed steps with inputs resident on the device
+e2e        the same through the public API (McClean.grad_run) with host
+           angles in (H2D) and host E + gradient out (D2H) every step
+roofline   dominant kernel (the backward sweep): FP64-bound on GB300, so the
+           roof is the measured FP64 FMA rate; the HBM view is reported too
+cpu_baseline  the CPU oracle (C + OpenMP restatement of the reference's
+           numpy algorithm) on the host cores, on a bounded sample
+--impl reference  times that CPU restatement as the reference arm
+
+Multi-GPU: replicas only (each rank runs its own circuit; no collective on
+the data path), launched with torchrun; rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--n", type=int, default=24)
+    ap.add_argument("--layers", type=int, default=50)
+    ap.add_argument("--dtype", default="complex128", choices=["complex128", "complex64"])
+    ap.add_argument("--entangler", default="cnot", choices=["cnot", "cz"])
+    ap.add_argument("--placement", default="before", choices=["before", "after"])
+    ap.add_argument("--grad-mode", default="auto", choices=["auto", "history", "uncompute"])
+    ap.add_argument("--seed", type=int, default=24)
+    ap.add_argument("--cpu-layers", type=int, default=10,
+                    help="layers of the bounded CPU-baseline sample (same n, axes, angles)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    return ap.parse_args()
+
+
+def workload(n, L, seed):
+    rng = np.random.default_rng(seed)
+    axes = rng.integers(0, 3, (L, n))
+    angles = rng.uniform(0, 2 * np.pi, (L, n))
+    zz = np.full((n, n), None)
+    for i in range(n - 1):
+        zz[i, i + 1] = 1.0
+    return axes, angles, {"zz": zz}
+
+
+def algorithmic(n, L, dtype):
+    """Per-circuit bytes and FP64/FP32 flops of the compulsory model:
+    B = S (6L + 4) (forward R+W per layer, observable, backward R+W of psi and
+    lambda per layer), F = 2^n (6 n (L+1) + 12 n L + 4 n L + 6)."""
+    S = (2 ** n) * (16 if dtype == "complex128" else 8)
+    B = S * (6 * L + 4)
+    F = (2 ** n) * (6 * n * (L + 1) + 12 * n * L + 4 * n * L + 6)
+    return B, F
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(n, L, axes, angles, layers):
+    """The CPU oracle (C + OpenMP restatement of the reference algorithm) on
+    the first `layers` layers of the same circuit; scaled to circuits/s of
+    the full L-layer circuit."""
+    from oracle import oracle as O
+
+    Ls = min(L, layers)
+    t = O.Terms(np.full(n - 1, 3), np.arange(n - 1), np.arange(1, n), np.ones(n - 1))
+    t0 = time.perf_counter()
+    O.mcclean_grad(n, axes[:Ls], angles[:Ls], t)
+    dt = time.perf_counter() - t0
+    per_layer = dt / Ls
+    return {"value": 1.0 / (per_layer * L), "unit": "circuits/s", "cores": O.num_threads(), "kind": "port",
+            "sample": "oracle/qg_oracle.c grad_run of the first %d of %d layers (n=%d), %.1f s, scaled by L" %
+                      (Ls, L, n, dt)}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    axes, angles, _ = workload(args.n, args.layers, args.seed)
+    from oracle import oracle as O
+
+    O.build()
+    Ls = min(args.layers, args.cpu_layers)
+    for _ in range(args.warmup):
+        cpu_baseline(args.n, args.layers, axes, angles, Ls)
+    times = []
+    for _ in range(args.steps):
+        r = cpu_baseline(args.n, args.layers, axes, angles, Ls)
+        times.append(1.0 / r["value"])
+    t = float(np.mean(times))
+    value = 1.0 / t
+    line = {"impl": "reference", "metric": "grad_run circuits/s", "value": value, "unit": "circuits/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded axes/angles)",
+            "config": config_of(args),
+            "cpu_baseline": {"value": value, "unit": "circuits/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": "circuits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def config_of(args):
+    return {"workload": "McClean grad_run n=%d L=%d %s, ZZ-chain observable, %s ladder %s rotations" %
+                        (args.n, args.layers, args.dtype, args.entangler, args.placement),
+            "n": args.n, "layers": args.layers, "entangler": args.entangler, "placement": args.placement,
+            "grad_mode": args.grad_mode, "seed": args.seed,
+            "l2": "inputs larger than L2 (state %d MiB > 129 MB)" % ((2 ** args.n) * (16 if args.dtype == "complex128"
+                                                                                      else 8) >> 20),
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from qradient_gb300 import McClean, _lib
+    from qradient_gb300._native import ptr, stream_handle
+
+    lib = _lib.load()
+    axes, angles, obs = workload(args.n, args.layers, args.seed + rank)
+    circ = McClean(args.n, obs, args.layers, axes=axes, angles=angles, dtype=args.dtype,
+                   entangler=args.entangler, placement=args.placement, grad_mode=args.grad_mode, device=dev)
+    angles_dev = torch.as_tensor(angles, dtype=torch.float64, device=dev).reshape(-1)
+    out = (torch.empty(1, dtype=torch.float64, device=dev),
+           torch.empty(args.n * args.layers, dtype=torch.float64, device=dev))
+
+    def step():
+        circ.grad_run_tensors(angles_dev, out=out)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    # FP64 roof: measured FMA rate of this GPU
+    scratch = torch.empty(1 << 20, dtype=torch.uint8, device=dev)
+    import ctypes
+
+    rate = ctypes.c_double(0.0)
+    _lib.check(lib.qg_probe_fp64_fma_rate(ptr(scratch), scratch.numel(), ctypes.byref(rate), stream_handle(dev)))
+    fp64_peak_tflops = 2.0 * rate.value * 1e-12
+
+    phys = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    idx = phys.split(",")[local] if phys else str(local)
+    clocks = ClockSampler(idx)
+    clocks.start()
+    lib.qg_profile_enable(1)
+    stream = torch.cuda.current_stream(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    kinfo = {}
+    for cls, name in ((0, "forward_sweep"), (1, "backward_sweep"), (2, "observable")):
+        tot = ctypes.c_double(0.0)
+        cnt = ctypes.c_int(0)
+        _lib.check(lib.qg_profile_collect(cls, ctypes.byref(tot), ctypes.byref(cnt)))
+        kinfo[name] = (tot.value, cnt.value)
+    lib.qg_profile_enable(0)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * 1e3 / ms_per_step
+
+    # end to end through the public API: host angles in, host E + grad out
+    e2e_s = float("nan")
+    if not args.no_e2e:
+        for _ in range(2):
+            circ.grad_run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            circ.angles = angles
+            E, g = circ.grad_run()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    B, F = algorithmic(args.n, args.layers, args.dtype)
+    # dominant kernel: the backward sweep.  Its algorithmic share per launch:
+    # reads psi and lambda, writes lambda per sweep; reductions (4 flop) and a
+    # rotation (6 flop) per amplitude per rotation.
+    bwd_ms, bwd_n = kinfo["backward_sweep"]
+    fwd_ms, fwd_n = kinfo["forward_sweep"]
+    S = (2 ** args.n) * (16 if args.dtype == "complex128" else 8)
+    per_launch_bytes = 3 * S
+    per_launch_flops = (2 ** args.n) * args.n * (4 + 6) * args.layers / max(bwd_n / args.steps, 1)
+    bwd_avg_s = bwd_ms / max(bwd_n, 1) * 1e-3
+    achieved_tflops = per_launch_flops / bwd_avg_s * 1e-12 if bwd_n else None
+    achieved_gbs = per_launch_bytes / bwd_avg_s * 1e-9 if bwd_n else None
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "backward_sweep_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("dram_bytes_per_launch")
+        except ValueError:
+            traffic = None
+    if args.dtype == "complex128":
+        roof = {"bound": "fp64", "kernel": "sweep_bwd_kernel<double,history>", "achieved": achieved_tflops,
+                "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                "frac": achieved_tflops / fp64_peak_tflops if achieved_tflops else None, "traffic": traffic,
+                "peak_source": "measured live: FP64 FMA chain probe (qg_probe_fp64_fma_rate) x 2",
+                "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                        "frac": achieved_gbs / hbm_peak if achieved_gbs else None,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+                "launch_ms_avg": bwd_avg_s * 1e3, "launches": bwd_n,
+                "kernel_share": {k: v[0] / ms for k, v in kinfo.items()}}
+    else:
+        roof = {"bound": "hbm", "kernel": "sweep_bwd_kernel<float,history>", "achieved": achieved_gbs,
+                "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak if achieved_gbs else None,
+                "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                "launch_ms_avg": bwd_avg_s * 1e3, "launches": bwd_n,
+                "kernel_share": {k: v[0] / ms for k, v in kinfo.items()}}
+
+    launches_per_step = (fwd_n + bwd_n + kinfo["observable"][1]) / args.steps + 1  # + the finalize kernel
+    line = {
+        "metric": "grad_run circuits/s", "value": value, "unit": "circuits/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.dtype == "complex128" else "f32",
+        "data": "synthetic (seeded axes/angles)", "config": config_of(args),
+        "hbm_gbs_algorithmic": B * value * 1e-9,
+        "fp64_tflops_algorithmic": F * value * 1e-12,
+        "e2e": {"value": world / e2e_s, "unit": "circuits/s", "h2d_bytes_per_step": angles.size * 8,
+                "d2h_bytes_per_step": (angles.size + 1) * 8},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "roofline": roof,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.n, args.layers, axes, angles, args.cpu_layers)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

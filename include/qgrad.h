@@ -122,6 +122,15 @@ int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t 
  * scratch_dev needs 1 MiB.  Synchronises the stream. */
 int qg_probe_fp64_fma_rate(void* scratch_dev, size_t scratch_bytes, double* fma_per_s, qg_stream stream);
 
+/* Launch timing for roofline reporting.  While enabled, the library records
+ * a CUDA event pair (on the launching stream) around every sweep launch of
+ * the calling thread; qg_profile_collect waits for them and returns the
+ * summed device time and launch count of one kernel class
+ * (0: forward sweeps, 1: backward sweeps, 2: observable passes) since the
+ * last qg_profile_enable(1). */
+int qg_profile_enable(int on);
+int qg_profile_collect(int kernel_class, double* total_ms, int* launches);
+
 const char* qg_status_string(int status);
 /* Message of the last failed call on this thread. */
 const char* qg_last_error(void);

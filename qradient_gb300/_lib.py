@@ -33,6 +33,8 @@ SIGNATURES = {
     "qg_sample_workspace_size": (_I, [_I, ctypes.POINTER(_SZ)]),
     "qg_sample": (_I, [_I, _I, _P, _I64, _U64, _U64, _P, _SZ, _P, _P]),
     "qg_probe_fp64_fma_rate": (_I, [_P, _SZ, ctypes.POINTER(ctypes.c_double), _P]),
+    "qg_profile_enable": (_I, [_I]),
+    "qg_profile_collect": (_I, [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "qg_status_string": (ctypes.c_char_p, [_I]),
     "qg_last_error": (ctypes.c_char_p, []),
     "qg_version": (_I, []),

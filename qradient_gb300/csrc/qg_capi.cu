@@ -302,6 +302,40 @@ int sm_count() {
 
 inline size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// ------------------------------------------------------------ launch timing
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool[3];
+  size_t used[3] = {0, 0, 0};
+  cudaEvent_t get(int cls) {
+    auto& p = pool[cls];
+    if (used[cls] == p.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      p.push_back(e);
+    }
+    return p[used[cls]++];
+  }
+};
+thread_local Profiler g_prof;
+
+struct ProfScope {
+  int cls;
+  cudaStream_t st;
+  ProfScope(int c, cudaStream_t s) : cls(c), st(s) {
+    if (g_prof.on) {
+      cudaEvent_t e = g_prof.get(cls);
+      if (e) cudaEventRecord(e, st);
+    }
+  }
+  ~ProfScope() {
+    if (g_prof.on) {
+      cudaEvent_t e = g_prof.get(cls);
+      if (e) cudaEventRecord(e, st);
+    }
+  }
+};
+
 struct WsLayout {
   size_t partials = 0, lam = 0, psi = 0, cost = 0, total = 0;
   size_t state_bytes = 0;
@@ -409,6 +443,7 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
     d->cost = (int8_t)c->cost_kind;
     d->cost_w0 = c->cost_w0;
     d->eslot = eslot0;
+    ProfScope ps(2, st);
     QG_CUDA(launch_observable<R>(*d, psi, lam, ci, cd, partials, W.G, W.G, st));
     return QG_OK;
   }
@@ -447,6 +482,7 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
     if (s > 0 && nxy == 0) continue;
     d->accumulate = s > 0;
     d->eslot = eslot0 + es++;
+    ProfScope ps(2, st);
     QG_CUDA(launch_observable<R>(*d, psi, lam, ci, cd, partials, W.G, W.G, st));
   }
   return QG_OK;
@@ -479,6 +515,7 @@ int forward(const qg_circuit* c, const Program& P, const WsLayout& W, const doub
     }
     p.psi_in = in;
     p.psi_out = out;
+    ProfScope ps(0, st);
     QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd, st));
     in = out;
   }
@@ -555,6 +592,7 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
       if (d.psi_undo == ENT_CNOT) pc ^= 1;
       p.psi_out = pbuf[pc];
     }
+    ProfScope ps(1, st);
     QG_CUDA(launch_sweep_bwd<R>(d, p, !history, W.G, st));
   }
   C* lam = lbuf[lc];
@@ -610,6 +648,27 @@ const char* qg_status_string(int s) {
 }
 
 const char* qg_last_error(void) { return g_last_error.c_str(); }
+
+int qg_profile_enable(int on) {
+  g_prof.on = on != 0;
+  for (int c = 0; c < 3; ++c) g_prof.used[c] = 0;
+  return QG_OK;
+}
+
+int qg_profile_collect(int cls, double* total_ms, int* launches) {
+  if (cls < 0 || cls > 2 || !total_ms || !launches) return fail(QG_ERR_INVALID, "bad profile query");
+  const size_t used = g_prof.used[cls];
+  double ms = 0.0;
+  for (size_t i = 0; i + 1 < used; i += 2) {
+    QG_CUDA(cudaEventSynchronize(g_prof.pool[cls][i + 1]));
+    float f = 0.f;
+    QG_CUDA(cudaEventElapsedTime(&f, g_prof.pool[cls][i], g_prof.pool[cls][i + 1]));
+    ms += f;
+  }
+  *total_ms = ms;
+  *launches = (int)(used / 2);
+  return QG_OK;
+}
 
 int qg_mcclean_create(int n, int layers, const int32_t* axes, int entangler, int placement, int nterms,
                       const int32_t* kind, const int32_t* q0, const int32_t* q1, const double* w, qg_circuit** out) {
