@@ -91,7 +91,7 @@ struct Layout {
 // high bits, each padded with the lowest bits (coalesced 128-byte runs).
 Layout make_layout(int n, int dtype) {
   Layout lay;
-  int t = dtype == QG_C128 ? env_int("QG_TILE_BITS_C128", 12) : env_int("QG_TILE_BITS_C64", 13);
+  int t = dtype == QG_C128 ? env_int("QG_TILE_BITS_C128", 11) : env_int("QG_TILE_BITS_C64", 12);
   t = std::max(4, std::min(t, TMAX));
   const int c = dtype == QG_C128 ? 3 : 4;
   if (n <= t) {
@@ -369,9 +369,16 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
   w.state_bytes = ((size_t)1 << n) * esz;
   const int64_t ntiles = (int64_t)1 << (n - P.lay.t);
   const int sms = sm_count();
-  const int per_sm = env_int("QG_CTAS_PER_SM", 1);
-  w.G = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_sm);
-  w.grid_fwd = (int)std::min<int64_t>(ntiles, (int64_t)sms * std::max(per_sm, 2));
+  // resident CTAs per SM of the largest (shared-memory-wise) sweep
+  SweepDesc big = P.sweeps[0];
+  for (const auto& d : P.sweeps)
+    if (d.nz > big.nz || (d.cost == COST_INT && big.cost != COST_INT)) big = d;
+  const bool unc = op == QG_OP_GRAD_UNCOMPUTE;
+  int per_bwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, true, unc) : sweep_ctas_per_sm<float>(big, true, unc);
+  int per_fwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, false, false) : sweep_ctas_per_sm<float>(big, false, false);
+  per_bwd = env_int("QG_CTAS_PER_SM", per_bwd);
+  w.G = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_bwd);
+  w.grid_fwd = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_fwd);
   w.neslots = obs_sweeps_needed(c, P.lay, op != QG_OP_RUN);
   const int m = (int)P.sweeps.size();
   w.pingpong = P.obs_pre == ENT_CNOT;

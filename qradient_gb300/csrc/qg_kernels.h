@@ -6,6 +6,10 @@
 
 namespace qg {
 
+// Resident CTAs per SM of a sweep kernel with this descriptor's shared memory.
+template <typename R>
+int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute);
+
 template <typename R>
 cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st);
 

@@ -71,28 +71,25 @@ __device__ __forceinline__ int sw<float>(int e) {
 
 __device__ __forceinline__ int insert0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
 
-template <typename C>
-__device__ __forceinline__ C cmul(C a, double2 b);
-template <>
-__device__ __forceinline__ double2 cmul<double2>(double2 a, double2 b) {
+// complex multiply / real scale in the state's own precision
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
-template <>
-__device__ __forceinline__ float2 cmul<float2>(float2 a, double2 b) {
-  const float bx = (float)b.x, by = (float)b.y;
-  return make_float2(fmaf(a.x, bx, -a.y * by), fmaf(a.x, by, a.y * bx));
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
+__device__ __forceinline__ double2 cscale(double2 a, double k) { return make_double2(a.x * k, a.y * k); }
+__device__ __forceinline__ float2 cscale(float2 a, float k) { return make_float2(a.x * k, a.y * k); }
 
 template <typename C>
-__device__ __forceinline__ C cscale(C a, double k);
+__device__ __forceinline__ C to_c(double2 v);
 template <>
-__device__ __forceinline__ double2 cscale<double2>(double2 a, double k) {
-  return make_double2(a.x * k, a.y * k);
+__device__ __forceinline__ double2 to_c<double2>(double2 v) {
+  return v;
 }
 template <>
-__device__ __forceinline__ float2 cscale<float2>(float2 a, double k) {
-  const float kf = (float)k;
-  return make_float2(a.x * kf, a.y * kf);
+__device__ __forceinline__ float2 to_c<float2>(double2 v) {
+  return make_float2((float)v.x, (float)v.y);
 }
 
 template <typename C>
@@ -110,7 +107,8 @@ __device__ __forceinline__ C load_pre(const C* psi, uint64_t x, int ent, const L
   return v;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
@@ -170,15 +168,22 @@ __device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u, R 
 
 // ------------------------------------------------------------ shared setup
 
+// reduction slots of one CTA: X/Y rotations, U_j of the Z rotations, the
+// element total T, the gamma reduction
+constexpr int RS_XY = 0, RS_Z = TMAX, RS_T = TMAX + ZMAX, RS_G = TMAX + ZMAX + 1, RS_N = TMAX + ZMAX + 2;
+
 struct SetupShared {
   double u[TMAX];
   double kappa[TMAX];
-  double K;        // product of the folded scale factors (diagonal sweeps)
+  double sc[QMAX];     // scale factors of the folded rotations
+  double zs[ZMAX], zc[ZMAX];
+  double K;  // product of the folded scale factors (diagonal sweeps)
   int form[TMAX];
+  int zk[ZMAX];        // Z rotation on a tile bit walked by the element loop: its k bit, else -1
   int64_t offhi[32];   // deposit(k << 8) for the element loop
   uint8_t outside[QMAX];
   double startP[QMAX + 1];
-  double red[NTHREADS / 32][TMAX + ZMAX + 2];
+  double red[NTHREADS / 32][RS_N];
 };
 
 // Deposit the low bits of v into the listed bit positions.
@@ -189,11 +194,11 @@ __device__ __forceinline__ int64_t deposit(int64_t v, const uint8_t* bits, int n
   return x;
 }
 
-// Common per-CTA setup: gate coefficients, element offsets, outside bits.
-// Also builds the diagonal phase table (Z rotations * scale) and the
-// integer-cost phase table when requested.
-template <bool BWD>
-__device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShared& S, double2* ztab, double2* ctab) {
+// Common per-CTA setup: gate coefficients, element offsets, outside bits,
+// the diagonal phase table (Z rotations * scale) and the integer-cost phase
+// table, both stored in the state's precision.
+template <typename C, bool BWD>
+__device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShared& S, C* ztab, C* ctab) {
   const int tid = threadIdx.x;
   const int t = d.t, n = d.n;
   if (tid < d.nxy) {
@@ -203,6 +208,14 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
     S.form[tid] = f;
     S.kappa[tid] = k;
   }
+  if (tid < d.nz) {
+    // local tile position of the Z rotation's bit
+    int zk = -1;
+    for (int i = 8; i < t; ++i)
+      if (d.bits[i] == d.z[tid].gbit) zk = i - 8;
+    S.zk[tid] = zk;
+  }
+  for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;
   if (t > 8) {
     for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
   } else if (tid == 0) {
@@ -222,47 +235,51 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
     // Ry(pi/4)|0> = cos(pi/8)|0> + sin(pi/8)|1> on every qubit
     double s8, c8;
     sincospi(0.125, &s8, &c8);
-    double p = 1.0;
-    for (int k = 0; k < n; ++k) p *= c8;
-    S.startP[0] = p;
-    for (int k = 1; k <= n; ++k) {
+    for (int k = 0; k <= n; ++k) {
       double q = 1.0;
       for (int i = 0; i < n - k; ++i) q *= c8;
       for (int i = 0; i < k; ++i) q *= s8;
       S.startP[k] = q;
     }
   }
+  // per-rotation scale factors and Z phases once per CTA, then the table
   if (d.has_diag) {
-    // scale K = prod kappa over the layer's X/Y rotations
-    double K = 1.0;
-    for (int i = 0; i < d.nscale; ++i) {
+    for (int i = tid; i < d.nscale; i += NTHREADS) {
       int f;
       double k;
       rot_form(angle_of(d.scale[i], params), &f, &k);
-      K *= k;
+      S.sc[i] = k;
     }
-    if (tid == 0) S.K = K;
+    if (tid < d.nz) sincos(0.5 * angle_of(d.z[tid].a, params), &S.zs[tid], &S.zc[tid]);
+  }
+  __syncthreads();
+  if (d.has_diag && tid == 0) {
+    double K = 1.0;
+    for (int i = 0; i < d.nscale; ++i) K *= S.sc[i];
+    S.K = K;
+  }
+  __syncthreads();
+  const double K = d.has_diag ? S.K : 1.0;
+  const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
+  if (d.has_diag && !fold) {
     const int nz = d.nz;
     for (int pat = tid; pat < (1 << nz); pat += NTHREADS) {
       double2 ph = make_double2(K, 0.0);
-      for (int j = 0; j < nz; ++j) {
-        double s, c;
-        sincos(0.5 * angle_of(d.z[j].a, params), &s, &c);
-        // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170)
-        const double2 e = make_double2(c, ((pat >> j) & 1) ? s : -s);
-        ph = cmul<double2>(ph, e);
-      }
+      // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170)
+      for (int j = 0; j < nz; ++j) ph = cmul(ph, make_double2(S.zc[j], ((pat >> j) & 1) ? S.zs[j] : -S.zs[j]));
       if (BWD) ph.y = -ph.y;
-      ztab[pat] = ph;
+      ztab[pat] = to_c<C>(ph);
     }
   }
   if (d.cost == COST_INT) {
+    // exp(-i gamma w0 m) (times the layer scale when folded)
     const double g = angle_of(d.cost_angle, params) * d.cost_w0;
+    const double kf = fold ? K : 1.0;
     const int M = d.cost_maxabs;
     for (int i = tid; i <= 2 * M; i += NTHREADS) {
       double s, c;
       sincos(g * (double)(i - M), &s, &c);
-      ctab[i] = make_double2(c, BWD ? s : -s);  // exp(-i gamma C) forward
+      ctab[i] = to_c<C>(make_double2(kf * c, kf * (BWD ? s : -s)));
     }
   }
   __syncthreads();
@@ -272,6 +289,35 @@ __device__ __forceinline__ int zpattern(uint64_t x, const SweepDesc& d) {
   int pat = 0;
   for (int j = 0; j < d.nz; ++j) pat |= (int)((x >> d.z[j].gbit) & 1) << j;
   return pat;
+}
+
+// Per-amplitude diagonal work of a sweep at index x: the cost phase and the
+// merged Z-rotation table (forward tables, or conjugated ones backward).
+template <typename C>
+__device__ __forceinline__ C apply_diag(C v, uint64_t x, const SweepDesc& d, const C* ztab, const C* ctab,
+                                        const int32_t* cost_i, const double* cost_d, double gamma, bool fold,
+                                        bool bwd) {
+  if (d.cost == COST_INT) {
+    v = cmul(v, ctab[cost_i[x] + d.cost_maxabs]);
+  } else if (d.cost == COST_REAL) {
+    double s, c;
+    sincos(gamma * cost_d[x], &s, &c);
+    v = cmul(v, to_c<C>(make_double2(c, bwd ? s : -s)));
+  }
+  if (d.has_diag && !fold) {
+    if (d.nz)
+      v = cmul(v, ztab[zpattern(x, d)]);
+    else
+      v = cscale(v, ztab[0].x);
+  }
+  return v;
+}
+
+// add a per-thread value into this warp's reduction slot
+template <typename R>
+__device__ __forceinline__ void red_add(SetupShared& S, int slot, R v) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) S.red[threadIdx.x >> 5][slot] += (double)v;
 }
 
 // ------------------------------------------------------------ forward sweep
@@ -284,9 +330,9 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   const int t = d.t, n = d.n;
   const int tsize = 1 << t;
   C* tile = (C*)smem;
-  double2* ztab = (double2*)(tile + tsize);
-  double2* ctab = ztab + (1 << d.nz);
-  sweep_setup<false>(d, p.params, S, ztab, ctab);
+  C* ztab = tile + tsize;
+  C* ctab = ztab + (1 << d.nz);
+  sweep_setup<C, false>(d, p.params, S, ztab, ctab);
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -294,9 +340,9 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int64_t ntiles = (int64_t)1 << (n - t);
-  const double plus = exp2(-0.5 * n);
-  const bool diag_folded = d.cost == COST_INT && d.has_diag && d.nz == 0;
-  const double kfold = diag_folded ? ztab[0].x : 1.0;
+  const R plus = (R)exp2(-0.5 * n);
+  const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
+  const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
 
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
@@ -304,8 +350,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        uint64_t src = x;
-        if (d.pre == ENT_CNOT) src = ladder_inv(x, lm);
+        const uint64_t src = d.pre == ENT_CNOT ? ladder_inv(x, lm) : x;
         C v;
         if (d.start == START_LOAD) {
           v = p.psi_in[src];
@@ -313,26 +358,11 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
           v.x = (R)S.startP[__popcll(src)];
           v.y = (R)0;
         } else {
-          v.x = (R)plus;
+          v.x = plus;
           v.y = (R)0;
         }
         if (d.pre == ENT_CZ && cz_negative(x)) v = cneg(v);
-        if (d.cost == COST_INT) {
-          double2 ph = ctab[p.cost_i[x] + d.cost_maxabs];
-          if (diag_folded) ph = make_double2(ph.x * kfold, ph.y * kfold);
-          v = cmul<C>(v, ph);
-        } else if (d.cost == COST_REAL) {
-          double s, c;
-          sincos(angle_of(d.cost_angle, p.params) * p.cost_d[x], &s, &c);
-          v = cmul<C>(v, make_double2(c, -s));
-        }
-        if (d.has_diag && !diag_folded) {
-          if (d.nz)
-            v = cmul<C>(v, ztab[zpattern(x, d)]);
-          else
-            v = cscale<C>(v, ztab[0].x);
-        }
-        tile[sw<R>(e)] = v;
+        tile[sw<R>(e)] = apply_diag<C>(v, x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
       }
     }
     __syncthreads();
@@ -367,6 +397,11 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
 // mc_clean.py:68-77: -2 Re<psi|(-i P/2) lam> = Im<lam|P|psi>), then applies
 // the inverse gates to lambda (and to psi when it is uncomputed rather than
 // read from the stored history).
+//
+// Z rotations: S_j = sum_x s_j(x) w_x with w_x = Im(conj(lam_x) psi_x) and
+// s_j = +1 on bit 0 is evaluated as T - 2 U_j (T = sum w, U_j = the sum over
+// bit j set).  U_j needs a per-element add only when bit j varies inside a
+// thread's element loop; otherwise the thread's tile total is added once.
 
 template <typename R, bool UNCOMPUTE>
 __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_constant__ SweepDesc d, SweepPtrs<R> p) {
@@ -377,9 +412,9 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   const int tsize = 1 << t;
   C* tl = (C*)smem;
   C* tp = tl + tsize;
-  double2* ztab = (double2*)(tp + tsize);
-  double2* ctab = ztab + (1 << d.nz);
-  sweep_setup<true>(d, p.params, S, ztab, ctab);
+  C* ztab = tp + tsize;
+  C* ctab = ztab + (1 << d.nz);
+  sweep_setup<C, true>(d, p.params, S, ztab, ctab);
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -387,30 +422,29 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int64_t ntiles = (int64_t)1 << (n - t);
-  const bool diag_folded = d.cost == COST_INT && d.has_diag && d.nz == 0;
-  const double kfold = diag_folded ? ztab[0].x : 1.0;
+  const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
+  const bool need_w = d.nz > 0 || d.gslot >= 0;
   // Uncomputing psi: the scaled inverse rotations return psi / kappa per
   // rotation, while the forward stored psi with the scale of the forward
   // scaled forms.  Keeping <lam|P|psi> unscaled at every sweep boundary needs
   // psi multiplied by (prod own kappa)^2 (/ K^2 on the diagonal sweep, where
   // the diagonal already multiplies by K).
-  double psi_mult = 1.0;
+  R psi_mult = (R)1;
   if (UNCOMPUTE) {
     double own = 1.0;
     for (int g = 0; g < d.nxy; ++g) own *= S.kappa[g];
-    psi_mult = own * own;
-    if (d.has_diag) psi_mult /= S.K * S.K;
+    double m = own * own;
+    if (d.has_diag) m /= S.K * S.K;
+    psi_mult = (R)m;
   }
-
-  double acc_xy[TMAX], acc_z[ZMAX], acc_g = 0.0;
-#pragma unroll
-  for (int i = 0; i < TMAX; ++i) acc_xy[i] = 0.0;
-#pragma unroll
-  for (int i = 0; i < ZMAX; ++i) acc_z[i] = 0.0;
 
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
+    R tT = (R)0, tG = (R)0;
+    R tU[ZMAX];
+#pragma unroll
+    for (int j = 0; j < ZMAX; ++j) tU[j] = (R)0;
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
@@ -420,45 +454,58 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
         C q = p.psi_in[d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x];
         if (d.lam_undo == ENT_CZ && cz_negative(x)) l = cneg(l);
         if (d.psi_undo == ENT_CZ && cz_negative(x)) q = cneg(q);
-        const double w = (double)l.x * (double)q.y - (double)l.y * (double)q.x;  // Im(conj(l) q)
-        if (d.gslot >= 0) {
-          const double cx = d.gcost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x];
-          acc_g = fma(cx, w, acc_g);
-        }
+        if (need_w) {
+          const R w = fma(l.x, q.y, -l.y * q.x);  // Im(conj(l) q)
+          tT += w;
 #pragma unroll
-        for (int j = 0; j < ZMAX; ++j)
-          if (j < d.nz) acc_z[j] += ((x >> d.z[j].gbit) & 1) ? -w : w;
+          for (int j = 0; j < ZMAX; ++j)
+            if (j < d.nz && S.zk[j] >= 0 && ((k >> S.zk[j]) & 1)) tU[j] += w;
+          if (d.gslot >= 0) {
+            const R cx = (R)(d.gcost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x]);
+            tG = fma(cx, w, tG);
+          }
+        }
         tl[sw<R>(e)] = l;
         tp[sw<R>(e)] = q;
       }
     }
+    if (d.nz > 0) {
+      const uint64_t x0 = (uint64_t)(base | dep_lo);
+#pragma unroll
+      for (int j = 0; j < ZMAX; ++j) {
+        if (j < d.nz) {
+          const R u = S.zk[j] >= 0 ? tU[j] : (((x0 >> d.z[j].gbit) & 1) && active ? tT : (R)0);
+          red_add<R>(S, RS_Z + j, u);
+        }
+      }
+      red_add<R>(S, RS_T, tT);
+    }
+    if (d.gslot >= 0) red_add<R>(S, RS_G, tG);
     __syncthreads();
     // gradient reductions for the X/Y rotations (read-only pass)
-#pragma unroll
-    for (int g = 0; g < TMAX; ++g) {
-      if (g < d.nxy) {
-        const int j = d.xy[g].lbit;
-        const bool isx = d.xy[g].axis == AX_X;
-        double a = 0.0;
-        for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
-          const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
-          const C la = tl[ia], lb = tl[ib], qa = tp[ia], qb = tp[ib];
-          if (isx) {
-            // Im(conj(la) qb) + Im(conj(lb) qa)
-            a = fma((double)la.x, (double)qb.y, a);
-            a = fma(-(double)la.y, (double)qb.x, a);
-            a = fma((double)lb.x, (double)qa.y, a);
-            a = fma(-(double)lb.y, (double)qa.x, a);
-          } else {
-            // Y: -Re(conj(la) qb) + Re(conj(lb) qa)
-            a = fma(-(double)la.x, (double)qb.x, a);
-            a = fma(-(double)la.y, (double)qb.y, a);
-            a = fma((double)lb.x, (double)qa.x, a);
-            a = fma((double)lb.y, (double)qa.y, a);
-          }
+#pragma unroll 1
+    for (int g = 0; g < d.nxy; ++g) {
+      const int j = d.xy[g].lbit;
+      const bool isx = d.xy[g].axis == AX_X;
+      R a = (R)0;
+      for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
+        const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
+        const C la = tl[ia], lb = tl[ib], qa = tp[ia], qb = tp[ib];
+        if (isx) {
+          // Im(conj(la) qb) + Im(conj(lb) qa)
+          a = fma(la.x, qb.y, a);
+          a = fma(-la.y, qb.x, a);
+          a = fma(lb.x, qa.y, a);
+          a = fma(-lb.y, qa.x, a);
+        } else {
+          // Y: -Re(conj(la) qb) + Re(conj(lb) qa)
+          a = fma(-la.x, qb.x, a);
+          a = fma(-la.y, qb.y, a);
+          a = fma(lb.x, qa.x, a);
+          a = fma(lb.y, qa.y, a);
         }
-        acc_xy[g] += a;
       }
+      red_add<R>(S, RS_XY + g, a);
     }
     __syncthreads();
     // inverse rotations
@@ -485,73 +532,36 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        const uint64_t z = x;
-        C l = tl[sw<R>(e)];
-        C q;
-        if (UNCOMPUTE) q = tp[sw<R>(e)];
-        // inverse diagonal and inverse cost phase at index z
-        if (d.has_diag && !diag_folded) {
-          if (d.nz) {
-            const double2 ph = ztab[zpattern(z, d)];
-            l = cmul<C>(l, ph);
-            if (UNCOMPUTE) q = cmul<C>(q, ph);
-          } else {
-            l = cscale<C>(l, ztab[0].x);
-            if (UNCOMPUTE) q = cscale<C>(q, ztab[0].x);
-          }
-        }
-        if (d.cost == COST_INT) {
-          double2 ph = ctab[p.cost_i[z] + d.cost_maxabs];
-          if (diag_folded) ph = make_double2(ph.x * kfold, ph.y * kfold);
-          l = cmul<C>(l, ph);
-          if (UNCOMPUTE) q = cmul<C>(q, ph);
-        } else if (d.cost == COST_REAL) {
-          double s, c;
-          sincos(gamma * p.cost_d[z], &s, &c);
-          l = cmul<C>(l, make_double2(c, s));
-          if (UNCOMPUTE) q = cmul<C>(q, make_double2(c, s));
-        }
-        p.lam_out[x] = l;
-        if (UNCOMPUTE) p.psi_out[x] = cscale<C>(q, psi_mult);
+        p.lam_out[x] = apply_diag<C>(tl[sw<R>(e)], x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true);
+        if (UNCOMPUTE)
+          p.psi_out[x] = cscale(apply_diag<C>(tp[sw<R>(e)], x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold,
+                                              true),
+                                psi_mult);
       }
     }
     __syncthreads();
   }
 
-  // block reduction of the gradient accumulators -> partials[slot][blockIdx]
-  const int warp = tid >> 5, lane = tid & 31;
-#pragma unroll
-  for (int g = 0; g < TMAX; ++g) {
-    if (g < d.nxy) {
-      const double v = warp_sum(acc_xy[g]);
-      if (lane == 0) S.red[warp][g] = v;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < ZMAX; ++j) {
-    if (j < d.nz) {
-      const double v = warp_sum(acc_z[j]);
-      if (lane == 0) S.red[warp][TMAX + j] = v;
-    }
-  }
-  if (d.gslot >= 0) {
-    const double v = warp_sum(acc_g);
-    if (lane == 0) S.red[warp][TMAX + ZMAX] = v;
-  }
-  __syncthreads();
-  if (tid < TMAX + ZMAX + 1) {
+  // CTA totals -> partials[slot][blockIdx]
+  if (tid < RS_N) {
     int slot = -1;
-    if (tid < TMAX) {
+    double sign = 1.0;
+    if (tid < RS_Z) {
       if (tid < d.nxy) slot = d.xy[tid].slot;
-    } else if (tid < TMAX + ZMAX) {
-      if (tid - TMAX < d.nz) slot = d.z[tid - TMAX].slot;
-    } else {
+    } else if (tid < RS_T) {
+      if (tid - RS_Z < d.nz) slot = d.z[tid - RS_Z].slot;
+      sign = -2.0;
+    } else if (tid == RS_G) {
       slot = d.gslot;
     }
     if (slot >= 0) {
-      double s = 0.0;
-      for (int w = 0; w < NTHREADS / 32; ++w) s += S.red[w][tid];
-      p.partials[(int64_t)slot * p.G + blockIdx.x] = s;
+      double s = 0.0, tot = 0.0;
+      for (int w = 0; w < NTHREADS / 32; ++w) {
+        s += S.red[w][tid];
+        tot += S.red[w][RS_T];
+      }
+      // Z rotations: S_j = T - 2 U_j
+      p.partials[(int64_t)slot * p.G + blockIdx.x] = tid >= RS_Z && tid < RS_T ? tot + sign * s : s;
     }
   }
 }
@@ -754,10 +764,35 @@ template <typename R>
 static size_t sweep_smem(const SweepDesc& d, bool bwd) {
   using C = typename C2T<R>::T;
   size_t s = (size_t)(bwd ? 2 : 1) * ((size_t)1 << d.t) * sizeof(C);
-  s += ((size_t)1 << d.nz) * sizeof(double2);
-  if (d.cost == COST_INT) s += (size_t)(2 * d.cost_maxabs + 1) * sizeof(double2);
+  s += ((size_t)1 << d.nz) * sizeof(C);
+  if (d.cost == COST_INT) s += (size_t)(2 * d.cost_maxabs + 1) * sizeof(C);
   return s;
 }
+
+template <typename R>
+int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute) {
+  const size_t smem = sweep_smem<R>(d, bwd);
+  int blocks = 0;
+  cudaError_t e;
+  if (!bwd) {
+    cudaFuncSetAttribute(sweep_fwd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_kernel<R>, NTHREADS, smem);
+  } else if (uncompute) {
+    cudaFuncSetAttribute(sweep_bwd_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, true>, NTHREADS, smem);
+  } else {
+    cudaFuncSetAttribute(sweep_bwd_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, false>, NTHREADS, smem);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return blocks > 0 ? blocks : 1;
+}
+
+template int sweep_ctas_per_sm<double>(const SweepDesc&, bool, bool);
+template int sweep_ctas_per_sm<float>(const SweepDesc&, bool, bool);
 
 template <typename R>
 cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st) {
