@@ -199,20 +199,19 @@ template cudaError_t launch_sample<float2>(int, const float2*, int64_t, uint64_t
 
 // ------------------------------------------------------------ FP64 probe
 
+// 16 independent FMA chains per thread, enough to cover the FP64 pipe latency
 __global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
-  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
-         x7 = x0 + 7;
+  double x[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) x[c] = threadIdx.x * 1e-3 + c;
   for (int i = 0; i < iters; ++i) {
-    x0 = fma(x0, a, b);
-    x1 = fma(x1, a, b);
-    x2 = fma(x2, a, b);
-    x3 = fma(x3, a, b);
-    x4 = fma(x4, a, b);
-    x5 = fma(x5, a, b);
-    x6 = fma(x6, a, b);
-    x7 = fma(x7, a, b);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) x[c] = fma(x[c], a, b);
   }
-  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
 cudaError_t probe_fp64(double* scratch, size_t bytes, double* rate, cudaStream_t st) {
@@ -228,18 +227,25 @@ cudaError_t probe_fp64(double* scratch, size_t bytes, double* rate, cudaStream_t
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int iters = 2048;
+  const int iters = 1024;
   dfma_probe_kernel<<<blocks, threads, 0, st>>>(scratch, 64, 1.0000001, 1e-9);
-  cudaEventRecord(e0, st);
-  dfma_probe_kernel<<<blocks, threads, 0, st>>>(scratch, iters, 1.0000001, 1e-9);
-  cudaEventRecord(e1, st);
-  e = cudaEventSynchronize(e1);
-  float ms = 0.f;
-  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, st);
+    dfma_probe_kernel<<<blocks, threads, 0, st>>>(scratch, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && ms > 0.f) {
+      const double r = (double)blocks * threads * iters * 16.0 / (ms * 1e-3);
+      if (r > best) best = r;
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return e;
-  *rate = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+  *rate = best;
   return cudaGetLastError();
 }
 
