@@ -117,6 +117,54 @@ int qg_sample_workspace_size(int n, size_t* bytes);
 int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t seed, uint64_t offset,
               void* workspace_dev, size_t workspace_bytes, int64_t* out_dev, qg_stream stream);
 
+/* ---- Batched persistent execution (no reference counterpart: the
+ * reference runs one circuit per Python call).  Many small circuits, each
+ * a whole run or grad_run with psi and lambda resident in shared memory,
+ * in one launch (CUDA-graph capturable).  Limits: complex64 n <= 14,
+ * complex128 n <= 13, L <= 4096, and for QAOA an integer cost with
+ * |m| <= 511. */
+typedef struct qg_term {
+  int32_t kind, q0, q1, pad; /* qg_pauli, qubits (q1 for ZZ) */
+  double w;
+} qg_term;
+
+typedef struct qg_cost_term {
+  int32_t b0, b1, c, pad; /* bit positions (b1 < 0: Z term) and integer coefficient */
+} qg_cost_term;
+
+/* One job; every pointer is device memory. */
+typedef struct qg_batch_job {
+  int32_t kind;        /* 0 McClean, 1 QAOA */
+  int32_t n, layers;
+  int32_t entangler;   /* McClean: qg_entangler */
+  int32_t placement;   /* McClean: qg_placement */
+  int32_t nterms;      /* observable terms */
+  const qg_term* terms;
+  const int8_t* axes;  /* McClean [layers * n] */
+  const double* params;/* McClean [layers * n]; QAOA [layers, 2] */
+  double* expec;       /* out: one double */
+  double* grad;        /* out: nparams doubles, or NULL for a run */
+  int32_t cost_nterms; /* QAOA cost C = cost_w0 * sum c_k s_k(x) */
+  int32_t cost_maxabs;
+  double cost_w0;
+  const qg_cost_term* cost;
+} qg_batch_job;
+
+/* QAOA integer cost of a term list (host): fills up to max_out cost terms,
+ * *w0 and *maxabs; QG_ERR_UNSUPPORTED when the weights have no common
+ * integer base. */
+int qg_qaoa_cost_terms(int n, int nterms, const int32_t* kind, const int32_t* q0, const int32_t* q1,
+                       const double* w, int max_out, qg_cost_term* out, int* nout, double* w0, int* maxabs);
+
+/* Workspace bytes for one batched launch. */
+int qg_batch_workspace_size(size_t* bytes);
+
+/* Run njobs jobs (jobs_dev: device array) in persistent launches.  All jobs
+ * must share dtype; max_qubits bounds their n (sets the shared-memory size).
+ * Jobs with n above the single-CTA limit use 2-CTA clusters. */
+int qg_batch_launch(int dtype, const qg_batch_job* jobs_dev, int njobs, int max_qubits, int cluster,
+                    void* workspace_dev, size_t workspace_bytes, qg_stream stream);
+
 /* Measured FP64 FMA issue rate of this GPU (FMA/s), for roofline
  * reporting: a dependent-chain DFMA kernel timed with CUDA events.
  * scratch_dev needs 1 MiB.  Synchronises the stream. */

@@ -1,0 +1,736 @@
+// Batched persistent kernel: many small circuits (different parameters,
+// qubit counts, depths, McClean or QAOA) in one launch.
+//
+// Each job is a whole run or adjoint grad_run (mc_clean.py:27-78,
+// qaoa.py:23-70) executed with psi and lambda resident in shared memory:
+// no state ever goes to HBM.  A CTA holds the whole state when it fits
+// (complex64 n <= 13, complex128 n <= 12); a 2-CTA cluster holds one state
+// split by its top bit (qubit 0) otherwise (complex64 n = 14, complex128
+// n = 13), and the only cross-CTA operations (rotations, reductions and X/Y
+// observable terms on qubit 0) read the partner CTA's shared memory
+// (distributed shared memory) between cluster barriers.  The CNOT ladder
+// never targets qubit 0, so it stays inside each CTA.
+//
+// Clusters (or CTAs) take jobs from a device counter until the queue is
+// empty (persistent grid, one launch per precision and cluster size; the
+// launch is CUDA-graph capturable).  The gradient uses the uncompute form of
+// the adjoint sweep (psi is rotated back instead of read from a history).
+#include <cooperative_groups.h>
+#include <stdint.h>
+
+#include "qg_batched.h"
+
+namespace cg = cooperative_groups;
+
+namespace qg {
+
+namespace {
+
+constexpr int BZMAX = 10;     // Z rotations merged per table (2^BZMAX = BATCH_TABLE entries)
+constexpr int BMAXQ = 26;
+
+__device__ __forceinline__ double2 cmulb(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cmulb(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+template <typename C>
+__device__ __forceinline__ C toc(double x, double y);
+template <>
+__device__ __forceinline__ double2 toc<double2>(double x, double y) {
+  return make_double2(x, y);
+}
+template <>
+__device__ __forceinline__ float2 toc<float2>(double x, double y) {
+  return make_float2((float)x, (float)y);
+}
+
+__device__ __forceinline__ int swb(int e, bool dbl) { return dbl ? e ^ (((e >> 3) & 1) * 7) : e ^ (((e >> 4) & 1) * 15); }
+__device__ __forceinline__ int ins0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
+
+__device__ __forceinline__ uint64_t lad_fwd(uint64_t x, uint64_t odd, uint64_t even) {
+  x ^= (x & odd) >> 1;
+  x ^= (x & even) >> 1;
+  return x;
+}
+__device__ __forceinline__ uint64_t lad_inv(uint64_t x, uint64_t odd, uint64_t even) {
+  x ^= (x & even) >> 1;
+  x ^= (x & odd) >> 1;
+  return x;
+}
+
+__device__ __forceinline__ double rform(double theta, int* form, double* kappa) {
+  double s, c;
+  sincos(0.5 * theta, &s, &c);
+  if (fabs(c) >= fabs(s)) {
+    *form = 0;
+    *kappa = c;
+    return s / c;
+  }
+  *form = 1;
+  *kappa = s;
+  return c / s;
+}
+
+// scaled-form rotation of the pair (a: bit 0, b: bit 1); sg = +1 / -1
+template <typename C, typename R>
+__device__ __forceinline__ void rotp(C& a, C& b, int axis, int form, R u, R sg) {
+  const C a0 = a, b0 = b;
+  if (axis == 0) {
+    if (form == 0) {
+      const R us = u * sg;
+      a.x = fma(us, b0.y, a0.x);
+      a.y = fma(-us, b0.x, a0.y);
+      b.x = fma(us, a0.y, b0.x);
+      b.y = fma(-us, a0.x, b0.y);
+    } else {
+      a.x = fma(u, a0.x, sg * b0.y);
+      a.y = fma(u, a0.y, -sg * b0.x);
+      b.x = fma(u, b0.x, sg * a0.y);
+      b.y = fma(u, b0.y, -sg * a0.x);
+    }
+  } else {
+    if (form == 0) {
+      const R us = u * sg;
+      a.x = fma(-us, b0.x, a0.x);
+      a.y = fma(-us, b0.y, a0.y);
+      b.x = fma(us, a0.x, b0.x);
+      b.y = fma(us, a0.y, b0.y);
+    } else {
+      a.x = fma(u, a0.x, -sg * b0.x);
+      a.y = fma(u, a0.y, -sg * b0.y);
+      b.x = fma(u, b0.x, sg * a0.x);
+      b.y = fma(u, b0.y, sg * a0.y);
+    }
+  }
+}
+
+// reduction term of one pair for Im<lam|P|psi>: X: Im(conj la qb) + Im(conj lb qa);
+// Y: -Re(conj la qb) + Re(conj lb qa)
+template <typename C, typename R>
+__device__ __forceinline__ R redp(const C& la, const C& lb, const C& qa, const C& qb, int axis) {
+  if (axis == 0) return fma(la.x, qb.y, -la.y * qb.x) + fma(lb.x, qa.y, -lb.y * qa.x);
+  return -fma(la.x, qb.x, la.y * qb.y) + fma(lb.x, qa.x, lb.y * qa.y);
+}
+
+template <typename R>
+__device__ __forceinline__ R wsum(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// G rotations on ascending local bits bits[0..G-1], each thread owning the
+// 2^G amplitudes of one task (all other bits fixed) in registers.
+template <typename C, typename R, int G, int NT, bool DBL>
+__device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, const int* axis, const int* form,
+                                          const double* u, R sg) {
+  const int ntask = M >> G;
+  int b[G];
+  int ax[G], fm[G];
+  R uu[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    b[i] = bits[i];
+    ax[i] = axis[i];
+    fm[i] = form[i];
+    uu[i] = (R)u[i];
+  }
+  for (int tk = threadIdx.x; tk < ntask; tk += NT) {
+    int base = tk;
+#pragma unroll
+    for (int i = 0; i < G; ++i) base = ins0(base, b[i]);
+    int idx[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      int x = base;
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+        if ((c >> i) & 1) x |= 1 << b[i];
+      idx[c] = swb(x, DBL);
+    }
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      C* w = pass ? v2 : v;
+      if (w == nullptr) break;
+      C el[1 << G];
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) el[c] = w[idx[c]];
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) rotp<C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i], sg);
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
+    }
+  }
+}
+
+struct BShared {
+  int job;
+  int nxy, nz, ncross;       // gates of the current layer
+  int xbit[BMAXQ];           // local bits of the X/Y rotations (cross rotation excluded)
+  int xaxis[BMAXQ];
+  int xslot[BMAXQ];          // output index
+  double xu[BMAXQ];
+  int xform[BMAXQ];
+  int caxis, cform, cslot;   // the cross rotation on the top bit (clusters)
+  double cu;
+  int zbit[BMAXQ];           // global bits of the Z rotations
+  int zslot[BMAXQ];
+  double zs[BMAXQ], zc[BMAXQ];
+  double K;
+  double startP[BMAXQ + 1];
+  double red[32][BMAXQ + 4];
+};
+
+}  // namespace
+
+template <typename R, int CS, int NT>
+__global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict__ jobs, int njobs, int* counter,
+                                                      int mmax) {
+  using C = typename BatchC<R>::T;
+  constexpr bool DBL = sizeof(R) == 8;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BShared S;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int Mmax = 1 << mmax;
+  C* psi = (C*)smem;
+  C* lam = psi + Mmax;
+  C* ztab = lam + Mmax;               // BATCH_TABLE entries: Z-rotation phases or QAOA cost phases
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = CS > 1 ? (int)cluster.block_rank() : 0;
+  C* rpsi = psi;
+  C* rlam = lam;
+  if (CS > 1) {
+    rpsi = cluster.map_shared_rank(psi, rank ^ 1);
+    rlam = cluster.map_shared_rank(lam, rank ^ 1);
+  }
+  auto csync = [&]() {
+    if (CS > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+
+  for (;;) {
+    if (tid == 0 && rank == 0) {
+      const int j = atomicAdd(counter, 1);
+      S.job = j;
+      if (CS > 1) *cluster.map_shared_rank(&S.job, 1) = j;
+    }
+    csync();
+    const int jid = S.job;
+    if (jid >= njobs) break;
+    const BatchJob J = jobs[jid];
+    const int n = J.n;
+    const int m = n - (CS > 1 ? 1 : 0);
+    const int M = 1 << m;
+    const uint64_t top = (uint64_t)rank << m;
+    const bool grad = J.grad != nullptr;
+    const int L = J.layers;
+    uint64_t lodd = 0, leven = 0;
+    for (int q = 0; q + 1 < n; ++q) {
+      const uint64_t b = 1ull << (n - 1 - q);
+      if (q & 1)
+        lodd |= b;
+      else
+        leven |= b;
+    }
+    if (tid == 0) {
+      double s8, c8;
+      sincospi(0.125, &s8, &c8);
+      for (int k = 0; k <= n; ++k) {
+        double q = 1.0;
+        for (int i = 0; i < n - k; ++i) q *= c8;
+        for (int i = 0; i < k; ++i) q *= s8;
+        S.startP[k] = q;
+      }
+    }
+    if (tid == 0 && rank == 0 && CS > 1) {
+      if (J.expec) *J.expec = 0.0;
+      if (grad) {
+        const int np = J.kind == 0 ? L * n : 2 * L;
+        for (int i = 0; i < np; ++i) J.grad[i] = 0.0;
+      }
+    }
+    __syncthreads();
+    // start state
+    const R plus = (R)exp2(-0.5 * n);
+    for (int e = tid; e < M; e += NT) {
+      const uint64_t x = top | (uint64_t)e;
+      C v;
+      v.x = J.kind == 0 ? (R)S.startP[__popcll(x)] : plus;
+      v.y = (R)0;
+      psi[swb(e, DBL)] = v;
+    }
+    __syncthreads();
+
+    // ---- helpers bound to this job
+    // layer setup: rotations of layer i into S (forward coefficients)
+    auto setup_layer = [&](int i) {
+      if (tid == 0) {
+        int nxy = 0, nz = 0;
+        S.ncross = 0;
+        for (int q = 0; q < n; ++q) {
+          const int axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
+          const int b = n - 1 - q;
+          const int slot = J.kind == 0 ? i * n + q : 2 * i;
+          if (axis == 2) {
+            S.zbit[nz] = b;
+            S.zslot[nz] = slot;
+            ++nz;
+          } else if (CS > 1 && b == m) {
+            S.ncross = 1;
+            S.caxis = axis;
+            S.cslot = slot;
+          } else {
+            S.xbit[nxy] = b;
+            S.xaxis[nxy] = axis;
+            S.xslot[nxy] = slot;
+            ++nxy;
+          }
+        }
+        // rotations of a layer commute: order the X/Y ones by bit so that the
+        // groups of three below see ascending bits
+        for (int a = 1; a < nxy; ++a)
+          for (int b = a; b > 0 && S.xbit[b] < S.xbit[b - 1]; --b) {
+            int t0 = S.xbit[b]; S.xbit[b] = S.xbit[b - 1]; S.xbit[b - 1] = t0;
+            t0 = S.xaxis[b]; S.xaxis[b] = S.xaxis[b - 1]; S.xaxis[b - 1] = t0;
+            t0 = S.xslot[b]; S.xslot[b] = S.xslot[b - 1]; S.xslot[b - 1] = t0;
+          }
+        S.nxy = nxy;
+        S.nz = nz;
+      }
+      __syncthreads();
+      // coefficients
+      const double beta = J.kind == 1 ? J.params[2 * i] : 0.0;
+      if (tid < S.nxy) {
+        const int q = n - 1 - S.xbit[tid];
+        const double th = J.kind == 0 ? J.params[i * n + q] : beta;
+        int f;
+        double k;
+        S.xu[tid] = rform(th, &f, &k);
+        S.xform[tid] = f;
+      }
+      if (tid == NT - 1 && S.ncross) {
+        const double th = J.kind == 0 ? J.params[i * n + 0] : beta;
+        int f;
+        double k;
+        S.cu = rform(th, &f, &k);
+        S.cform = f;
+      }
+      if (tid < S.nz) {
+        const int q = n - 1 - S.zbit[tid];
+        sincos(0.5 * J.params[i * n + q], &S.zs[tid], &S.zc[tid]);
+      }
+      if (tid == 32) {
+        // K = product of the X/Y scale factors of the layer
+        double K = 1.0;
+        for (int q = 0; q < n; ++q) {
+          const int axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
+          if (axis == 2) continue;
+          const double th = J.kind == 0 ? J.params[i * n + q] : beta;
+          int f;
+          double k;
+          rform(th, &f, &k);
+          K *= k;
+        }
+        S.K = K;
+      }
+      __syncthreads();
+    };
+    // diagonal of layer i (Z table * K; QAOA cost phase * K); conj for the inverse
+    auto build_diag = [&](int i, bool inv) {
+      const int nzt = S.nz < BZMAX ? S.nz : BZMAX;
+      if (J.kind == 0) {
+        for (int pat = tid; pat < (1 << nzt); pat += NT) {
+          double2 ph = make_double2(S.K, 0.0);
+          for (int j = 0; j < nzt; ++j)
+            ph = cmulb(ph, make_double2(S.zc[j], ((pat >> j) & 1) ? S.zs[j] : -S.zs[j]));
+          ztab[pat] = toc<C>(ph.x, inv ? -ph.y : ph.y);
+        }
+      } else {
+        const double g = J.params[2 * i + 1] * J.cost_w0;
+        const int MA = J.cost_maxabs;
+        for (int k = tid; k <= 2 * MA; k += NT) {
+          double s, c;
+          sincos(g * (double)(k - MA), &s, &c);
+          ztab[k] = toc<C>(S.K * c, S.K * (inv ? s : -s));
+        }
+      }
+      __syncthreads();
+    };
+    auto cost_m = [&](uint64_t x) {
+      int mm = 0;
+      for (int k = 0; k < J.cost_nterms; ++k) {
+        const qg_cost_term t = J.cost[k];
+        int s = (int)((x >> t.b0) & 1);
+        if (t.b1 >= 0) s ^= (int)((x >> t.b1) & 1);
+        mm += s ? -t.c : t.c;
+      }
+      return mm;
+    };
+    // per-element diagonal multiply on buffer v (table built by build_diag)
+    auto apply_diag = [&](C* v, bool inv) {
+      const int nzt = S.nz < BZMAX ? S.nz : BZMAX;
+      for (int e = tid; e < M; e += NT) {
+        const uint64_t x = top | (uint64_t)e;
+        C a = v[swb(e, DBL)];
+        if (J.kind == 0) {
+          int pat = 0;
+          for (int j = 0; j < nzt; ++j) pat |= (int)((x >> S.zbit[j]) & 1) << j;
+          a = cmulb(a, ztab[pat]);
+          for (int j = BZMAX; j < S.nz; ++j) {
+            const bool one = (x >> S.zbit[j]) & 1;
+            const double sgn = (one != inv) ? 1.0 : -1.0;
+            a = cmulb(a, toc<C>(S.zc[j], sgn * S.zs[j]));
+          }
+        } else {
+          a = cmulb(a, ztab[cost_m(x) + J.cost_maxabs]);
+        }
+        v[swb(e, DBL)] = a;
+      }
+      __syncthreads();
+    };
+    // entangler on buffer v: (E v)[y] = v[A^{-1} y] (inverse: v[A y]); CZ sign
+    auto entangle = [&](C* v, bool inv) {
+      if (J.entangler == 2) {
+        for (int e = tid; e < M; e += NT) {
+          const uint64_t x = top | (uint64_t)e;
+          if (__popcll(x & (x >> 1)) & 1) {
+            C a = v[swb(e, DBL)];
+            a.x = -a.x;
+            a.y = -a.y;
+            v[swb(e, DBL)] = a;
+          }
+        }
+        __syncthreads();
+        return;
+      }
+      C tmp[BatchC<R>::EPT];
+#pragma unroll
+      for (int k = 0; k < BatchC<R>::EPT; ++k) {
+        const int e = tid + k * NT;
+        if (e < M) {
+          const uint64_t x = top | (uint64_t)e;
+          const uint64_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
+          tmp[k] = v[swb((int)(src & (uint64_t)(M - 1)), DBL)];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < BatchC<R>::EPT; ++k) {
+        const int e = tid + k * NT;
+        if (e < M) v[swb(e, DBL)] = tmp[k];
+      }
+      __syncthreads();
+    };
+    // X/Y rotations of the layer in groups of up to 3 bits per shared-memory pass
+    auto rotate = [&](C* v, C* v2, R sg) {
+      const int nxy = S.nxy;
+      for (int g0 = 0; g0 < nxy; g0 += 3) {
+        const int g = nxy - g0 < 3 ? nxy - g0 : 3;
+        if (g == 3)
+          rot_group<C, R, 3, NT, DBL>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sg);
+        else if (g == 2)
+          rot_group<C, R, 2, NT, DBL>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sg);
+        else
+          rot_group<C, R, 1, NT, DBL>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sg);
+        __syncthreads();
+      }
+      if (CS > 1 && S.ncross) {
+        // rotation on the top bit: the partner amplitude lives in the other CTA
+        cluster.sync();
+        C na[BatchC<R>::EPT], nb[BatchC<R>::EPT];
+#pragma unroll
+        for (int k = 0; k < BatchC<R>::EPT; ++k) {
+          const int e = tid + k * NT;
+          if (e < M) {
+            const C own = v[swb(e, DBL)];
+            const C rem = (v == psi ? rpsi : rlam)[swb(e, DBL)];
+            C x0 = rank == 0 ? own : rem, x1 = rank == 0 ? rem : own;
+            rotp<C, R>(x0, x1, S.caxis, S.cform, (R)S.cu, sg);
+            na[k] = rank == 0 ? x0 : x1;
+            if (v2) {
+              const C own2 = v2[swb(e, DBL)];
+              const C rem2 = (v2 == psi ? rpsi : rlam)[swb(e, DBL)];
+              C y0 = rank == 0 ? own2 : rem2, y1 = rank == 0 ? rem2 : own2;
+              rotp<C, R>(y0, y1, S.caxis, S.cform, (R)S.cu, sg);
+              nb[k] = rank == 0 ? y0 : y1;
+            }
+          }
+        }
+        cluster.sync();
+#pragma unroll
+        for (int k = 0; k < BatchC<R>::EPT; ++k) {
+          const int e = tid + k * NT;
+          if (e < M) {
+            v[swb(e, DBL)] = na[k];
+            if (v2) v2[swb(e, DBL)] = nb[k];
+          }
+        }
+        cluster.sync();
+      }
+    };
+    // block-sum of one value into the job's output (with 2 CTAs: two atomic
+    // adds onto 0, whose result does not depend on their order)
+    auto emit1 = [&](R val, int slot, double factor) {
+      const R v = wsum(val);
+      if (lane == 0) S.red[warp][0] = (double)v;
+      __syncthreads();
+      if (tid == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < NT / 32; ++w) tot += S.red[w][0];
+        tot *= factor;
+        if (CS > 1)
+          atomicAdd(&J.grad[slot], tot);
+        else
+          J.grad[slot] = tot;
+      }
+      __syncthreads();
+    };
+
+    // ---- forward
+    for (int i = 0; i < L; ++i) {
+      setup_layer(i);
+      if (J.kind == 0 && J.entangler != 0 && J.placement == 0) entangle(psi, false);
+      build_diag(i, false);
+      apply_diag(psi, false);
+      if (CS > 1) cluster.sync();
+      rotate(psi, nullptr, (R)1);
+      if (J.kind == 0 && J.entangler != 0 && J.placement == 1) entangle(psi, false);
+    }
+    if (CS > 1) cluster.sync();
+
+    // ---- observable: lam = O psi and E = Re<psi|lam>
+    {
+      R eacc = (R)0;
+      const bool costonly = J.kind == 1 && grad;
+      for (int e = tid; e < M; e += NT) {
+        const uint64_t x = top | (uint64_t)e;
+        const C v = psi[swb(e, DBL)];
+        R lx = (R)0, ly = (R)0;
+        if (costonly) {
+          const R d = (R)(J.cost_w0 * (double)cost_m(x));
+          lx = d * v.x;
+          ly = d * v.y;
+        } else {
+          for (int k = 0; k < J.nterms; ++k) {
+            const BatchTerm t = J.terms[k];
+            const uint64_t b0 = 1ull << (n - 1 - t.q0);
+            if (t.kind >= 2) {
+              bool s = (x & b0) != 0;
+              if (t.kind == 3) s ^= (x & (1ull << (n - 1 - t.q1))) != 0;
+              const R w = (R)(s ? -t.w : t.w);
+              lx = fma(w, v.x, lx);
+              ly = fma(w, v.y, ly);
+            } else {
+              const uint64_t xp = x ^ b0;
+              C u;
+              if ((xp >> m) != (x >> m))
+                u = rpsi[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
+              else
+                u = psi[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
+              const R w = (R)t.w;
+              if (t.kind == 0) {
+                lx = fma(w, u.x, lx);
+                ly = fma(w, u.y, ly);
+              } else {
+                const R sgn = (x & b0) ? (R)1 : (R)-1;
+                lx = fma(-sgn * w, u.y, lx);
+                ly = fma(sgn * w, u.x, ly);
+              }
+            }
+          }
+        }
+        eacc = fma(v.x, lx, fma(v.y, ly, eacc));
+        if (grad) {
+          C o;
+          o.x = lx;
+          o.y = ly;
+          lam[swb(e, DBL)] = o;
+        }
+      }
+      const R v = wsum(eacc);
+      if (lane == 0) S.red[warp][0] = (double)v;
+      __syncthreads();
+      if (tid == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < NT / 32; ++w) tot += S.red[w][0];
+        if (CS > 1)
+          atomicAdd(J.expec, tot);
+        else
+          *J.expec = tot;
+      }
+      __syncthreads();
+    }
+    if (CS > 1) cluster.sync();
+
+    // ---- backward (uncompute form)
+    if (grad) {
+      for (int i = L - 1; i >= 0; --i) {
+        setup_layer(i);
+        if (J.kind == 0 && J.entangler != 0 && J.placement == 1) {
+          entangle(psi, true);
+          entangle(lam, true);
+          if (CS > 1) cluster.sync();
+        }
+        // reductions at the end point of the layer's rotations; per-warp sums in S.red[warp][k]
+        const int nxy = S.nxy;
+        for (int gi = 0; gi < nxy; ++gi) {
+          const int j = S.xbit[gi];
+          R a = (R)0;
+          for (int pp = tid; pp < M / 2; pp += NT) {
+            const int ia = swb(ins0(pp, j), DBL), ib = swb(ins0(pp, j) | (1 << j), DBL);
+            a += redp<C, R>(lam[ia], lam[ib], psi[ia], psi[ib], S.xaxis[gi]);
+          }
+          a = wsum(a);
+          if (lane == 0) S.red[warp][gi] = (double)a;
+        }
+        int ns = nxy;
+        if (CS > 1 && S.ncross) {
+          R a = (R)0;
+          for (int e = tid; e < M; e += NT) {
+            const C l = lam[swb(e, DBL)];
+            const C qr = rpsi[swb(e, DBL)];
+            // rank 0 holds the bit-0 half (a), rank 1 the bit-1 half (b)
+            if (S.caxis == 0)
+              a += fma(l.x, qr.y, -l.y * qr.x);
+            else
+              a += rank == 0 ? -fma(l.x, qr.x, l.y * qr.y) : fma(l.x, qr.x, l.y * qr.y);
+          }
+          a = wsum(a);
+          if (lane == 0) S.red[warp][ns] = (double)a;
+          ++ns;
+        }
+        // Z rotations: sum_x s_j(x) Im(conj lam psi) = T - 2 U_j.  With
+        // e = tid + NT k, a Z bit below log2(NT) is fixed per thread, a bit
+        // above it is a bit of k (at most 4 of them), the top bit is the rank.
+        const int nz = S.nz;
+        if (nz > 0) {
+          constexpr int LGNT = NT == 512 ? 9 : (NT == 256 ? 8 : 10);
+          R T = (R)0;
+          R Uk[4] = {(R)0, (R)0, (R)0, (R)0};
+          for (int e = tid, k = 0; e < M; e += NT, ++k) {
+            const C l = lam[swb(e, DBL)], q = psi[swb(e, DBL)];
+            const R w = fma(l.x, q.y, -l.y * q.x);
+            T += w;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if ((k >> i) & 1) Uk[i] += w;
+          }
+          for (int j = 0; j < nz; ++j) {
+            const int b = S.zbit[j];
+            R U;
+            if (b < LGNT)
+              U = ((tid >> b) & 1) ? T : (R)0;
+            else if (b < m)
+              U = (b - LGNT == 0) ? Uk[0] : (b - LGNT == 1) ? Uk[1] : (b - LGNT == 2) ? Uk[2] : Uk[3];
+            else
+              U = rank ? T : (R)0;
+            R val = wsum(T - (R)2 * U);
+            if (lane == 0) S.red[warp][ns + j] = (double)val;
+          }
+          ns += nz;
+        }
+        __syncthreads();
+        if (J.kind == 0) {
+          if (tid < ns) {
+            double tot = 0.0;
+            for (int w = 0; w < NT / 32; ++w) tot += S.red[w][tid];
+            const int slot = tid < nxy ? S.xslot[tid] : (tid < nxy + ((CS > 1 && S.ncross) ? 1 : 0) ? S.cslot
+                                                                                                    : S.zslot[tid - nxy - ((CS > 1 && S.ncross) ? 1 : 0)]);
+            if (CS > 1)
+              atomicAdd(&J.grad[slot], tot);
+            else
+              J.grad[slot] = tot;
+          }
+        } else if (tid == 0) {
+          // beta: the sum over all n X rotations of the layer
+          double tot = 0.0;
+          for (int k = 0; k < ns; ++k)
+            for (int w = 0; w < NT / 32; ++w) tot += S.red[w][k];
+          if (CS > 1)
+            atomicAdd(&J.grad[2 * i], tot);
+          else
+            J.grad[2 * i] = tot;
+        }
+        __syncthreads();
+        // the partner may still read this CTA's psi for its top-bit reduction
+        if (CS > 1) cluster.sync();
+        // inverse rotations on lam and psi
+        rotate(lam, psi, (R)-1);
+        if (J.kind == 1) {
+          // gamma at the point after the cost phase (= before it: C commutes)
+          R gsum = (R)0;
+          for (int e = tid; e < M; e += NT) {
+            const uint64_t x = top | (uint64_t)e;
+            const C l = lam[swb(e, DBL)], q = psi[swb(e, DBL)];
+            gsum = fma((R)(J.cost_w0 * (double)cost_m(x)), fma(l.x, q.y, -l.y * q.x), gsum);
+          }
+          emit1(gsum, 2 * i + 1, 2.0);
+        }
+        build_diag(i, true);
+        apply_diag(lam, true);
+        apply_diag(psi, true);
+        if (J.kind == 0 && J.entangler != 0 && J.placement == 0) {
+          entangle(psi, true);
+          entangle(lam, true);
+        }
+        if (CS > 1) cluster.sync();
+      }
+    }
+    csync();
+  }
+}
+
+template <typename R, int CS>
+static cudaError_t launch_one(const BatchJob* jobs, int njobs, int* counter, int mmax, cudaStream_t st,
+                              int* grid_out) {
+  using C = typename BatchC<R>::T;
+  constexpr int NT = BATCH_THREADS;
+  const size_t smem = (size_t)(2 * (1 << mmax) + BATCH_TABLE) * sizeof(C);
+  auto kern = batched_kernel<R, CS, NT>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, NT, smem);
+  if (e != cudaSuccess) return e;
+  if (per < 1) return cudaErrorInvalidConfiguration;
+  int units = sms * per / CS;                 // clusters (or CTAs) resident at once
+  if (units > njobs) units = njobs;
+  if (units < 1) units = 1;
+  *grid_out = units;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(units * CS);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, jobs, njobs, counter, mmax);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batched(int dtype_double, int cluster, const BatchJob* jobs, int njobs, int* counter, int mmax,
+                           cudaStream_t st, int* grid_out) {
+  if (dtype_double) {
+    if (cluster == 2) return launch_one<double, 2>(jobs, njobs, counter, mmax, st, grid_out);
+    return launch_one<double, 1>(jobs, njobs, counter, mmax, st, grid_out);
+  }
+  if (cluster == 2) return launch_one<float, 2>(jobs, njobs, counter, mmax, st, grid_out);
+  return launch_one<float, 1>(jobs, njobs, counter, mmax, st, grid_out);
+}
+
+}  // namespace qg

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/qgrad.h"
+#include "qg_batched.h"
 #include "qg_extra.h"
 #include "qg_internal.cuh"
 #include "qg_kernels.h"
@@ -879,6 +880,64 @@ int qg_sample(int n, int dtype, const void* state, int64_t nshots, uint64_t seed
     QG_CUDA(launch_sample<float2>(n, (const float2*)state, nshots, seed, offset, (double*)ws, out, st));
   else
     return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+  return QG_OK;
+}
+
+int qg_qaoa_cost_terms(int n, int nterms, const int32_t* kind, const int32_t* q0, const int32_t* q1,
+                       const double* w, int max_out, qg_cost_term* out, int* nout, double* w0_out, int* maxabs_out) {
+  if (!nout || !w0_out || !maxabs_out || (max_out > 0 && !out)) return fail(QG_ERR_INVALID, "null output");
+  std::vector<Term> terms;
+  if (int st = parse_terms(n, nterms, kind, q0, q1, w, terms)) return st;
+  std::vector<Term> diag;
+  for (const auto& t : terms)
+    if (t.kind >= QG_PAULI_Z) diag.push_back(t);
+  double w0 = 0.0;
+  for (const auto& t : diag)
+    if (t.w != 0.0 && (w0 == 0.0 || fabs(t.w) < w0)) w0 = fabs(t.w);
+  if (diag.empty()) w0 = 1.0;
+  long maxabs = 0;
+  int k = 0;
+  for (const auto& t : diag) {
+    const double r = t.w / w0;
+    const double c = nearbyint(r);
+    if (!(fabs(r - c) == 0.0 && c * w0 == t.w && fabs(c) <= 1 << 20))
+      return fail(QG_ERR_UNSUPPORTED, "cost weights have no common integer base");
+    if (k >= max_out) return fail(QG_ERR_UNSUPPORTED, "more than %d cost terms", max_out);
+    out[k].b0 = n - 1 - t.q0;
+    out[k].b1 = t.kind == QG_PAULI_ZZ ? n - 1 - t.q1 : -1;
+    out[k].c = (int32_t)c;
+    out[k].pad = 0;
+    maxabs += labs((long)c);
+    ++k;
+  }
+  *nout = k;
+  *w0_out = w0;
+  *maxabs_out = (int)maxabs;
+  return QG_OK;
+}
+
+int qg_batch_workspace_size(size_t* bytes) {
+  if (!bytes) return fail(QG_ERR_INVALID, "null output");
+  *bytes = 256;
+  return QG_OK;
+}
+
+int qg_batch_launch(int dtype, const qg_batch_job* jobs, int njobs, int max_qubits, int cluster, void* ws,
+                    size_t wsb, qg_stream stream) {
+  if (njobs < 0) return fail(QG_ERR_INVALID, "negative job count");
+  if (njobs == 0) return QG_OK;
+  if (!jobs || !ws) return fail(QG_ERR_INVALID, "null pointer");
+  if (wsb < 256) return fail(QG_ERR_WORKSPACE, "workspace %zu bytes < 256 needed", wsb);
+  if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+  if (cluster != 1 && cluster != 2) return fail(QG_ERR_INVALID, "cluster must be 1 or 2");
+  const int mlimit = dtype == QG_C128 ? BatchC<double>::MMAX : BatchC<float>::MMAX;
+  const int m = max_qubits - (cluster - 1);
+  if (max_qubits < 1 || m > mlimit)
+    return fail(QG_ERR_UNSUPPORTED, "batched jobs need n <= %d (cluster %d)", mlimit + cluster - 1, cluster);
+  cudaStream_t st = (cudaStream_t)stream;
+  QG_CUDA(cudaMemsetAsync(ws, 0, sizeof(int), st));
+  int grid = 0;
+  QG_CUDA(launch_batched(dtype == QG_C128, cluster, jobs, njobs, (int*)ws, m < 1 ? 1 : m, st, &grid));
   return QG_OK;
 }
 
