@@ -67,7 +67,7 @@ def test_batch_qaoa_and_mixed_sizes():
 
     b = Batch(dtype="complex128")
     qcases = []
-    for n, p, seed in ((6, 2, 1), (10, 3, 2), (13, 2, 3), (16, 2, 4)):
+    for n, p, seed in ((6, 2, 1), (10, 3, 2), (12, 2, 3), (16, 2, 4)):
         edges = random_regular_edges(3, n, seed)
         q = Qaoa(n, MaxCut(n, edge_set=edges).to_observable(), p)
         rng = np.random.default_rng(seed)
