@@ -52,6 +52,11 @@ def parse():
                     help="layers of the bounded CPU-baseline sample (same n, axes, angles)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--workload", default="mcclean", choices=["mcclean", "batched", "qaoa"],
+                    help="mcclean: one n=24 L=50 circuit (headline); batched: 4096 parameter vectors of an "
+                         "n=14 L=30 circuit in one graph replay; qaoa: 3-regular MaxCut grad_run")
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--p", type=int, default=10, help="QAOA depth")
     return ap.parse_args()
 
 
@@ -194,10 +199,88 @@ def config_of(args):
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 
+def run_batched(args):
+    """4096 parameter vectors (uniform [0, 2 pi)) of one McClean circuit with
+    shared random axes, n=14, L=30, complex64 by default, in one CUDA-graph
+    replay of the persistent shared-memory kernel; compared with the plain
+    per-call GPU path (one grad_run at a time through the sweep kernels)."""
+    import torch
+
+    from qradient_gb300 import McClean
+    from qradient_gb300.batched import mcclean_batch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, L, B = args.n, args.layers, args.batch
+    rng = np.random.default_rng(args.seed + rank)
+    axes = rng.integers(0, 3, (L, n))
+    zz = np.full((n, n), None)
+    for i in range(n - 1):
+        zz[i, i + 1] = 1.0
+    b = mcclean_batch(n, L, axes, {"zz": zz}, B, dtype=args.dtype, device=dev)
+    P = torch.tensor(rng.uniform(0, 2 * np.pi, (B, L * n)), dtype=torch.float64, device=dev)
+    b.params_flat.copy_(P.reshape(-1))
+    for _ in range(max(args.warmup, 3)):
+        b.grad()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.current_stream(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.grad()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = B * 1e3 / ms
+    # plain per-call GPU path: the same circuit, one grad_run call per parameter vector
+    c = McClean(n, {"zz": zz}, L, axes=axes, angles=P[0].reshape(L, n).cpu().numpy(), dtype=args.dtype, device=dev)
+    for _ in range(3):
+        c.grad_run_tensors(angles=P[0])
+    torch.cuda.synchronize()
+    nplain = min(B, 64)
+    e0.record(stream)
+    for k in range(nplain):
+        c.grad_run_tensors(angles=P[k])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain = nplain * 1e3 / e0.elapsed_time(e1)
+    # end to end: host parameters in, host E + gradients out, per replay
+    Ph = P.cpu().pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.params_flat.copy_(Ph.reshape(-1), non_blocking=True)
+        E, _ = b.grad()
+        Eh = E.cpu()
+        Gh = b.grads_flat.cpu()
+    torch.cuda.synchronize()
+    e2e = B * args.steps / (time.perf_counter() - t0)
+    line = {"metric": "batched grad_run circuits/s", "value": value, "unit": "circuits/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.dtype == "complex64" else "f64",
+            "data": "synthetic (seeded axes/angles)",
+            "config": {"workload": "McClean grad_run n=%d L=%d %s, %d parameter vectors, shared axes, one CUDA-graph "
+                                   "replay of the persistent shared-memory kernel" % (n, L, args.dtype, B),
+                       "l2": "states live in shared memory; the %d x %d parameter block streams once" % (B, L * n)},
+            "plain_per_call_circuits_s": plain, "speedup_vs_plain": value / plain,
+            "e2e": {"value": e2e, "unit": "circuits/s", "h2d_bytes_per_step": B * L * n * 8,
+                    "d2h_bytes_per_step": B * (L * n + 1) * 8},
+            "gpu_launches": args.steps, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     import torch
 
     world, rank, local = dist_setup()

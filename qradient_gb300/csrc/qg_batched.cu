@@ -663,8 +663,12 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
         if (CS > 1) cluster.sync();
         // inverse rotations on lam and psi
         rotate(lam, psi, (R)-1);
+        build_diag(i, true);
+        apply_diag(lam, true);
+        apply_diag(psi, true);
         if (J.kind == 1) {
-          // gamma at the point after the cost phase (= before it: C commutes)
+          // gamma at the point before the cost phase (qaoa.py:65-68), where
+          // lambda and psi carry no scale factor
           R gsum = (R)0;
           for (int e = tid; e < M; e += NT) {
             const uint64_t x = top | (uint64_t)e;
@@ -673,9 +677,6 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
           }
           emit1(gsum, 2 * i + 1, 2.0);
         }
-        build_diag(i, true);
-        apply_diag(lam, true);
-        apply_diag(psi, true);
         if (J.kind == 0 && J.entangler != 0 && J.placement == 0) {
           entangle(psi, true);
           entangle(lam, true);
