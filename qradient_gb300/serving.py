@@ -1,0 +1,231 @@
+"""Continuous-batching request server for run / grad_run.
+
+Requests (a McClean or Qaoa circuit, its parameters, 'run' or 'grad', a
+dtype) arrive over time.  Each scheduling round:
+
+1. completed work is retired: results copied to the host, latency recorded,
+   its device memory returned to the admission budget;
+2. queued requests are admitted in arrival order while their device
+   footprint fits the budget (an adjoint request needs its workspace: psi and
+   lambda, doubled when the CNOT ladder needs ping-pong buffers; requests
+   that fit the shared-memory kernel need only their parameters and
+   outputs);
+3. admitted small requests are packed into one batched persistent launch
+   (``qg_batch_launch``), each admitted large request gets its own stream
+   running the sweep kernels.  Work from different rounds overlaps on the
+   device: a round never waits for earlier launches.
+
+Results are identical to running the request alone (same kernels, same
+reduction order); ``tests/test_gpu_serving.py`` checks this.
+"""
+import collections
+import time
+
+import numpy as np
+import torch
+
+from . import _lib, _native
+from .batched import CLUSTER_MAX, Batch
+
+
+class Request:
+    __slots__ = ("rid", "circuit", "params", "op", "dtype", "t_arrival", "t_done", "expec", "grad", "state",
+                 "footprint", "_e", "_g", "_event", "_keep")
+
+    def __init__(self, rid, circuit, params, op="grad", dtype="complex128", t_arrival=None):
+        self.rid = rid
+        self.circuit = circuit
+        self.params = np.asarray(params, dtype=np.float64)
+        if op not in ("grad", "run"):
+            raise ValueError("op must be 'grad' or 'run'")
+        self.op = op
+        self.dtype = _native.dtype_code(dtype)
+        self.t_arrival = time.perf_counter() if t_arrival is None else t_arrival
+        self.t_done = None
+        self.expec = None
+        self.grad = None
+        self.footprint = 0
+        self._event = None
+        self._keep = None
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_arrival
+
+    @property
+    def done(self):
+        return self.t_done is not None
+
+
+def _state_bytes(n, dtype):
+    return (2 ** n) * (16 if dtype == _lib.QG_C128 else 8)
+
+
+class Server:
+    """Admission by device-memory footprint, batched small requests, one
+    stream per large request (up to ``streams`` concurrently)."""
+
+    def __init__(self, device=None, hbm_budget=None, streams=4, max_batch=4096):
+        self.device = _native.require_cuda(device)
+        if hbm_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            hbm_budget = int(0.5 * free)
+        self.budget = int(hbm_budget)
+        self.in_use = 0
+        self.max_batch = max_batch
+        self.queue = collections.deque()
+        self.inflight = []
+        self.finished = []
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(streams)]
+        self.stream_busy = [None] * streams
+        self.batch_stream = torch.cuda.Stream(self.device)
+        self._rid = 0
+
+    # ------------------------------------------------------------ interface
+    def submit(self, circuit, params, op="grad", dtype="complex128", t_arrival=None):
+        r = Request(self._rid, circuit, params, op, dtype, t_arrival)
+        self._rid += 1
+        self._size(r)
+        if r.footprint > self.budget:
+            raise MemoryError("request needs %d bytes, above the server budget %d" % (r.footprint, self.budget))
+        self.queue.append(r)
+        return r
+
+    def _small(self, r):
+        kind = r.circuit.__class__.__name__
+        return r.circuit.qnum <= CLUSTER_MAX[r.dtype] and kind in ("McClean", "Qaoa")
+
+    def _size(self, r):
+        n = r.circuit.qnum
+        if self._small(r):
+            np_ = r.params.size
+            r.footprint = 8 * (2 * np_ + 1) + 4096
+        else:
+            op = _lib.QG_OP_GRAD_UNCOMPUTE if r.op == "grad" else _lib.QG_OP_RUN
+            r.footprint = r.circuit.native().workspace_bytes(r.dtype, op) + 8 * (2 * r.params.size + 1)
+
+    # ------------------------------------------------------------ scheduling
+    def _retire(self):
+        still = []
+        for item in self.inflight:
+            event, reqs, keep = item
+            if not event.query():
+                still.append(item)
+                continue
+            now = time.perf_counter()
+            for r in reqs:
+                r.expec = float(r._e.item())
+                if r.op == "grad":
+                    shape = (r.circuit.lnum, r.circuit.qnum) if r.circuit.__class__.__name__ == "McClean" else (
+                        r.circuit.lnum, 2)
+                    r.grad = r._g.cpu().numpy().reshape(shape)
+                r.t_done = now
+                self.in_use -= r.footprint
+                r._e = r._g = None
+                self.finished.append(r)
+            for i, s in enumerate(self.stream_busy):
+                if s is item:
+                    self.stream_busy[i] = None
+                    # large request finished: give its workspace back
+                    for r in reqs:
+                        if r.circuit._native is not None:
+                            r.circuit._native.release_workspaces()
+        self.inflight = still
+
+    def _admit(self):
+        small, large = [], []
+        free_streams = sum(1 for s in self.stream_busy if s is None)
+        while self.queue:
+            r = self.queue[0]
+            if self.in_use + r.footprint > self.budget:
+                break  # admission in arrival order: wait for memory to free up
+            if not self._small(r) and len(large) >= free_streams:
+                break  # no free stream for another large request yet
+            self.queue.popleft()
+            self.in_use += r.footprint
+            (small if self._small(r) else large).append(r)
+            if len(small) >= self.max_batch:
+                break
+        return small, large
+
+    def _launch_small(self, reqs):
+        by_dtype = collections.defaultdict(list)
+        for r in reqs:
+            by_dtype[r.dtype].append(r)
+        with torch.cuda.stream(self.batch_stream):
+            for dt, rs in by_dtype.items():
+                b = Batch(device=self.device, dtype=dt, grad=any(r.op == "grad" for r in rs), use_graph=False)
+                for r in rs:
+                    b.add(r.circuit, params=r.params.reshape(-1))
+                b.finalize()
+                b.execute()
+                for k, r in enumerate(rs):
+                    r._e = b.expec[k:k + 1]
+                    r._g = b.grads[k]
+                ev = torch.cuda.Event()
+                ev.record(self.batch_stream)
+                self.inflight.append((ev, rs, b))
+
+    def _launch_large(self, r):
+        idx = next(i for i, s in enumerate(self.stream_busy) if s is None)
+        st = self.streams[idx]
+        nat = r.circuit.native()
+        with torch.cuda.stream(st):
+            params = torch.as_tensor(r.params.reshape(-1)).to(self.device, non_blocking=False)
+            if r.op == "grad":
+                ws = nat.workspace(r.dtype, _lib.QG_OP_GRAD_UNCOMPUTE, self.device)
+                e, g = nat.grad(params, r.dtype, self.device, _lib.QG_OP_GRAD_UNCOMPUTE, workspace=ws)
+            else:
+                ws = nat.workspace(r.dtype, _lib.QG_OP_RUN, self.device)
+                e, _ = nat.run(params, r.dtype, self.device, workspace=ws)
+                g = None
+            r._e, r._g = e, g
+            ev = torch.cuda.Event()
+            ev.record(st)
+        item = (ev, [r], (params, ws))
+        self.stream_busy[idx] = item
+        self.inflight.append(item)
+
+    def step(self):
+        """One scheduling round; returns the number of requests admitted."""
+        self._retire()
+        small, large = self._admit()
+        if small:
+            self._launch_small(small)
+        for r in large:
+            self._launch_large(r)
+        return len(small) + len(large)
+
+    def drain(self, timeout=600.0):
+        t0 = time.perf_counter()
+        while self.queue or self.inflight:
+            if not self.step():
+                time.sleep(0.0002)
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError("server did not drain")
+        return self.finished
+
+    # ------------------------------------------------------------ workloads
+    def serve(self, schedule):
+        """Replay (t_offset, circuit, params, op, dtype) arrivals in real time
+        and return the finished requests."""
+        schedule = sorted(schedule, key=lambda s: s[0])
+        t0 = time.perf_counter()
+        i = 0
+        while i < len(schedule) or self.queue or self.inflight:
+            now = time.perf_counter() - t0
+            while i < len(schedule) and schedule[i][0] <= now:
+                off, c, p, op, dt = schedule[i]
+                self.submit(c, p, op, dt, t_arrival=t0 + off)
+                i += 1
+            if not self.step():
+                time.sleep(0.0002)
+        return self.finished
+
+
+def latency_stats(reqs):
+    lat = np.array([r.latency for r in reqs if r.latency is not None]) * 1e3
+    if lat.size == 0:
+        return {}
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "n": int(lat.size)}
