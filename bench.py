@@ -52,11 +52,13 @@ def parse():
                     help="layers of the bounded CPU-baseline sample (same n, axes, angles)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--workload", default="mcclean", choices=["mcclean", "batched", "qaoa"],
+    ap.add_argument("--workload", default="mcclean", choices=["mcclean", "batched", "qaoa", "serving"],
                     help="mcclean: one n=24 L=50 circuit (headline); batched: 4096 parameter vectors of an "
                          "n=14 L=30 circuit in one graph replay; qaoa: 3-regular MaxCut grad_run")
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--p", type=int, default=10, help="QAOA depth")
+    ap.add_argument("--requests", type=int, default=120, help="serving: requests in the Poisson stream")
+    ap.add_argument("--rate", type=float, default=0.0, help="serving: arrivals per second (0: saturate)")
     return ap.parse_args()
 
 
@@ -275,12 +277,161 @@ def run_batched(args):
         print(json.dumps(line))
 
 
+def run_qaoa(args):
+    """QAOA MaxCut grad_run on a seeded random 3-regular graph (n=24, p=10
+    by default, complex128), plus 100 Philox shots from the final state."""
+    import torch
+
+    from qradient_gb300 import Qaoa
+    from qradient_gb300.optimization_problems import MaxCut, random_regular_edges
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, p = args.n, args.p
+    edges = random_regular_edges(3, n, args.seed + rank)
+    rng = np.random.default_rng(args.seed + rank)
+    betas, gammas = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)
+    q = Qaoa(n, MaxCut(n, edge_set=edges).to_observable(), p, dtype=args.dtype, device=dev,
+             grad_mode=args.grad_mode)
+    params = torch.tensor(np.stack([betas, gammas], 1).reshape(-1), device=dev)
+    nat = q.native()
+    op = q._grad_op(nat)
+    for _ in range(max(args.warmup, 3)):
+        nat.grad(params, q._dtype_code, dev, op)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.current_stream(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        nat.grad(params, q._dtype_code, dev, op)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    q.run_expec_val(betas, gammas)
+    shots = q.sample(100, seed=args.seed).cpu().numpy()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        E, g = q.grad_run(betas, gammas)
+    e2e = args.steps / (time.perf_counter() - t0)
+    S = (2 ** n) * (16 if args.dtype == "complex128" else 8)
+    line = {"metric": "QAOA grad_run circuits/s", "value": 1e3 / ms * world, "unit": "circuits/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.dtype == "complex128" else "f32",
+            "data": "synthetic (seeded random 3-regular graph, beta/gamma uniform [0, pi))",
+            "config": {"workload": "QAOA MaxCut grad_run n=%d p=%d %s, %d edges" % (n, p, args.dtype, len(edges)),
+                       "l2": "inputs larger than L2" if S > 129e6 else "state fits in L2"},
+            "hbm_gbs_algorithmic": S * (6 * p + 4) / ms * 1e-6,
+            "shots_mean_cost": float(np.mean(q.classical_ham()[shots])) if n <= 26 else None,
+            "e2e": {"value": e2e, "unit": "circuits/s", "h2d_bytes_per_step": 2 * p * 8,
+                    "d2h_bytes_per_step": (2 * p + 1) * 8},
+            "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def serving_mix(seed, count):
+    """Config-5 request mix: 60% McClean n ~ U{8..26}, L ~ U{5..60}; 40% QAOA
+    3-regular MaxCut n ~ U{10..24} (even), p ~ U{1..6}; dtype per request."""
+    from qradient_gb300 import McClean, Qaoa
+    from qradient_gb300.optimization_problems import MaxCut, random_regular_edges
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        dtype = "complex128" if rng.random() < 0.5 else "complex64"
+        op = "grad" if rng.random() < 0.7 else "run"
+        if rng.random() < 0.6:
+            n = int(rng.integers(8, 27))
+            L = int(rng.integers(5, 61))
+            zz = np.full((n, n), None)
+            for i in range(n - 1):
+                zz[i, i + 1] = 1.0
+            c = McClean(n, {"zz": zz}, L, axes=rng.integers(0, 3, (L, n)), angles=np.zeros((L, n)), dtype=dtype,
+                        grad_mode="uncompute")
+            prm = rng.uniform(0, 2 * np.pi, (L, n))
+        else:
+            n = int(rng.integers(5, 13)) * 2
+            p = int(rng.integers(1, 7))
+            c = Qaoa(n, MaxCut(n, edge_set=random_regular_edges(3, n, seed * 1000 + k)).to_observable(), p,
+                     dtype=dtype, grad_mode="uncompute")
+            prm = np.stack([rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)], axis=1)
+        reqs.append((c, prm, op, dtype))
+    return reqs
+
+
+def run_serving(args):
+    """Poisson stream of the config-5 mix through the continuous-batching
+    server; compared with the plain per-call GPU path on the same requests."""
+    import torch
+
+    from qradient_gb300 import McClean
+    from qradient_gb300.serving import Server, latency_stats
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    reqs = serving_mix(args.seed + rank, args.requests)
+    # plain per-call path: one request at a time through the public API
+    def alone(c, prm, op):
+        if isinstance(c, McClean):
+            c.angles = prm
+            return c.grad_run() if op == "grad" else c.run_expec_val()
+        return c.grad_run(prm[:, 0], prm[:, 1]) if op == "grad" else c.run_expec_val(prm[:, 0], prm[:, 1])
+    for c, prm, op, dt in reqs[:4]:
+        alone(c, prm, op)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c, prm, op, dt in reqs:
+        alone(c, prm, op)
+        if c._native is not None:
+            c._native.release_workspaces()
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain = len(reqs) / plain_s
+    rate = args.rate if args.rate > 0 else 4.0 * plain  # saturating arrival rate
+    rng = np.random.default_rng(args.seed + 7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    srv = Server(device=dev, streams=4)
+    # warm-up round (kernel attributes, lazy module loading)
+    srv.serve([(0.0, c, prm, op, dt) for c, prm, op, dt in reqs[:4]])
+    srv.finished.clear()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    done = srv.serve([(float(a), c, prm, op, dt) for a, (c, prm, op, dt) in zip(arrivals, reqs)])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = latency_stats(done)
+    value = len(done) / wall
+    line = {"metric": "served circuits/s (run + grad_run mix)", "value": value * world, "unit": "circuits/s",
+            "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed f64/f32", "data": "synthetic Poisson stream",
+            "config": {"workload": "config-5 mix: 60%% McClean n~U{8..26} L~U{5..60}, 40%% QAOA 3-regular "
+                                   "n~U{10..24} p~U{1..6}, 70%% grad_run / 30%% run, dtype per request; "
+                                   "%d requests, Poisson rate %.1f/s" % (len(reqs), rate)},
+            "latency": st, "plain_per_call_circuits_s": plain, "speedup_vs_plain": value / plain,
+            "e2e": {"value": value * world, "unit": "circuits/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None}, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "qaoa":
+        return run_qaoa(args)
+    if args.workload == "serving":
+        return run_serving(args)
     import torch
 
     world, rank, local = dist_setup()
