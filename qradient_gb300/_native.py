@@ -25,6 +25,8 @@ _TORCH = {_lib.QG_C128: torch.complex128, _lib.QG_C64: torch.complex64}
 
 
 def dtype_code(dtype):
+    if isinstance(dtype, int) and not isinstance(dtype, bool) and dtype in (_lib.QG_C128, _lib.QG_C64):
+        return dtype
     try:
         return _DTYPES[dtype]
     except (KeyError, TypeError):
