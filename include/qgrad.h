@@ -165,6 +165,21 @@ int qg_batch_workspace_size(size_t* bytes);
 int qg_batch_launch(int dtype, const qg_batch_job* jobs_dev, int njobs, int max_qubits, int cluster,
                     void* workspace_dev, size_t workspace_bytes, qg_stream stream);
 
+/* ---- Allocation-free gradient (no counterpart in the reference).
+ * For callers that cannot allocate device memory where they need a
+ * gradient (inside a CUDA-graph capture, under a host that owns every
+ * device allocation, in a loop that forbids allocation after start-up).
+ * Same inputs and outputs as qg_grad in uncompute mode, but the scratch is a
+ * library-owned static device array of QG_NOALLOC_SCRATCH_BYTES that every
+ * GPU loading the library holds until exit.  Circuits whose uncompute
+ * workspace exceeds it get QG_ERR_UNSUPPORTED.  The first call on a device
+ * looks up the array's address; make it before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race, so order them (one
+ * stream). */
+#define QG_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
+int qg_grad_noalloc(const qg_circuit* c, int dtype, const double* params_dev, const void* ini_state_dev,
+                    double* expec_dev, double* grad_dev, qg_stream stream);
+
 /* Measured FP64 FMA issue rate of this GPU (FMA/s), for roofline
  * reporting: a dependent-chain DFMA kernel timed with CUDA events.
  * scratch_dev needs 1 MiB.  Synchronises the stream. */

@@ -37,6 +37,7 @@ SIGNATURES = {
                                ctypes.POINTER(_I)]),
     "qg_batch_workspace_size": (_I, [ctypes.POINTER(_SZ)]),
     "qg_batch_launch": (_I, [_I, _P, _I, _I, _I, _P, _SZ, _P]),
+    "qg_grad_noalloc": (_I, [_P, _I, _P, _P, _P, _P, _P]),
     "qg_profile_enable": (_I, [_I]),
     "qg_profile_collect": (_I, [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "qg_status_string": (ctypes.c_char_p, [_I]),

@@ -633,6 +633,10 @@ int parse_terms(int n, int nterms, const int32_t* kind, const int32_t* q0, const
 
 }  // namespace
 
+namespace qg {
+int set_last_error(int status, const char* msg) { return fail(status, "%s", msg); }
+}  // namespace qg
+
 extern "C" {
 
 int qg_version(void) { return 1; }

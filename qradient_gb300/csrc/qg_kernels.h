@@ -6,6 +6,9 @@
 
 namespace qg {
 
+// Record a failure message for qg_last_error() and return the status.
+int set_last_error(int status, const char* msg);
+
 // Resident CTAs per SM of a sweep kernel with this descriptor's shared memory.
 template <typename R>
 int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute);
