@@ -207,6 +207,9 @@ int build_layer(int n, const Layout& lay, const std::vector<LayerGate>& g, int8_
     z.a = g[q].a;
     d.has_diag = 1;
   }
+  // the rotations of a sweep commute: order them by local bit for the gate groups
+  for (auto& d : sw)
+    std::sort(d.xy, d.xy + d.nxy, [](const XYGate& a, const XYGate& b) { return a.lbit < b.lbit; });
   sw[0].pre = pre;  // entangler preceding this layer's rotations, gathered on load
   for (auto& d : sw) out.push_back(d);
   for (auto& d : extra) out.push_back(d);

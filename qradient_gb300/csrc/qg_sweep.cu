@@ -320,6 +320,126 @@ __device__ __forceinline__ void red_add(SetupShared& S, int slot, R v) {
   if ((threadIdx.x & 31) == 0) S.red[threadIdx.x >> 5][slot] += (double)v;
 }
 
+// ------------------------------------------------------------ gate groups
+//
+// The X/Y rotations of a sweep are sorted by local bit.  A group of G of them
+// (bits b0 < b1 < b2) is applied with each thread holding the 2^G amplitudes
+// of one task (all other tile bits fixed) in registers: one shared-memory
+// round trip and one barrier per group instead of per rotation.
+
+template <typename C, typename R, int G>
+__device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S, int g0,
+                                            R sg) {
+  int b[G], ax[G], fm[G];
+  R uu[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    b[i] = d.xy[g0 + i].lbit;
+    ax[i] = d.xy[g0 + i].axis;
+    fm[i] = S.form[g0 + i];
+    uu[i] = (R)S.u[g0 + i];
+  }
+  const int ntask = tsize >> G;
+  for (int tk = threadIdx.x; tk < ntask; tk += NTHREADS) {
+    int base = tk;
+#pragma unroll
+    for (int i = 0; i < G; ++i) base = insert0(base, b[i]);
+    int idx[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      int x = base;
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+        if ((c >> i) & 1) x |= 1 << b[i];
+      idx[c] = sw<R>(x);
+    }
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      C* w = pass ? v2 : v;
+      if (w == nullptr) break;
+      C el[1 << G];
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) el[c] = w[idx[c]];
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) rot_pair<C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i], sg);
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
+    }
+  }
+}
+
+// Im<lam|P|psi> pair term: X: Im(conj la qb) + Im(conj lb qa);
+// Y: -Re(conj la qb) + Re(conj lb qa)
+template <typename C, typename R>
+__device__ __forceinline__ R red_pair(const C& la, const C& lb, const C& qa, const C& qb, int axis, R a) {
+  if (axis == AX_X) {
+    a = fma(la.x, qb.y, a);
+    a = fma(-la.y, qb.x, a);
+    a = fma(lb.x, qa.y, a);
+    a = fma(-lb.y, qa.x, a);
+  } else {
+    a = fma(-la.x, qb.x, a);
+    a = fma(-la.y, qb.y, a);
+    a = fma(lb.x, qa.x, a);
+    a = fma(lb.y, qa.y, a);
+  }
+  return a;
+}
+
+// gradient reductions of a group of G rotations (read-only)
+template <typename C, typename R, int G>
+__device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize, const SweepDesc& d,
+                                             SetupShared& S, int g0) {
+  int b[G], ax[G];
+  R acc[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    b[i] = d.xy[g0 + i].lbit;
+    ax[i] = d.xy[g0 + i].axis;
+    acc[i] = (R)0;
+  }
+  const int ntask = tsize >> G;
+  for (int tk = threadIdx.x; tk < ntask; tk += NTHREADS) {
+    int base = tk;
+#pragma unroll
+    for (int i = 0; i < G; ++i) base = insert0(base, b[i]);
+    C la[1 << G], qa[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      int x = base;
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+        if ((c >> i) & 1) x |= 1 << b[i];
+      la[c] = tl[sw<R>(x)];
+      qa[c] = tp[sw<R>(x)];
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i)
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c)
+        if (!((c >> i) & 1)) acc[i] = red_pair<C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], ax[i], acc[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < G; ++i) red_add<R>(S, RS_XY + g0 + i, acc[i]);
+}
+
+template <typename C, typename R>
+__device__ __forceinline__ void apply_all(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S, R sg) {
+  for (int g0 = 0; g0 < d.nxy; g0 += 3) {
+    const int g = d.nxy - g0 < 3 ? d.nxy - g0 : 3;
+    if (g == 3)
+      apply_group<C, R, 3>(v, v2, tsize, d, S, g0, sg);
+    else if (g == 2)
+      apply_group<C, R, 2>(v, v2, tsize, d, S, g0, sg);
+    else
+      apply_group<C, R, 1>(v, v2, tsize, d, S, g0, sg);
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------ forward sweep
 
 template <typename R>
@@ -366,19 +486,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
       }
     }
     __syncthreads();
-#pragma unroll 1
-    for (int g = 0; g < d.nxy; ++g) {
-      const int j = d.xy[g].lbit, axis = d.xy[g].axis, form = S.form[g];
-      const R u = (R)S.u[g];
-      for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
-        const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
-        C a = tile[ia], b = tile[ib];
-        rot_pair<C, R>(a, b, axis, form, u, (R)1);
-        tile[ia] = a;
-        tile[ib] = b;
-      }
-      __syncthreads();
-    }
+    apply_all<C, R>(tile, nullptr, tsize, d, S, (R)1);
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
@@ -483,51 +591,18 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
     if (d.gslot >= 0) red_add<R>(S, RS_G, tG);
     __syncthreads();
     // gradient reductions for the X/Y rotations (read-only pass)
-#pragma unroll 1
-    for (int g = 0; g < d.nxy; ++g) {
-      const int j = d.xy[g].lbit;
-      const bool isx = d.xy[g].axis == AX_X;
-      R a = (R)0;
-      for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
-        const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
-        const C la = tl[ia], lb = tl[ib], qa = tp[ia], qb = tp[ib];
-        if (isx) {
-          // Im(conj(la) qb) + Im(conj(lb) qa)
-          a = fma(la.x, qb.y, a);
-          a = fma(-la.y, qb.x, a);
-          a = fma(lb.x, qa.y, a);
-          a = fma(-lb.y, qa.x, a);
-        } else {
-          // Y: -Re(conj(la) qb) + Re(conj(lb) qa)
-          a = fma(-la.x, qb.x, a);
-          a = fma(-la.y, qb.y, a);
-          a = fma(lb.x, qa.x, a);
-          a = fma(lb.y, qa.y, a);
-        }
-      }
-      red_add<R>(S, RS_XY + g, a);
+    for (int g0 = 0; g0 < d.nxy; g0 += 3) {
+      const int g = d.nxy - g0 < 3 ? d.nxy - g0 : 3;
+      if (g == 3)
+        reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+      else if (g == 2)
+        reduce_group<C, R, 2>(tl, tp, tsize, d, S, g0);
+      else
+        reduce_group<C, R, 1>(tl, tp, tsize, d, S, g0);
     }
     __syncthreads();
-    // inverse rotations
-#pragma unroll 1
-    for (int g = d.nxy - 1; g >= 0; --g) {
-      const int j = d.xy[g].lbit, axis = d.xy[g].axis, form = S.form[g];
-      const R u = (R)S.u[g];
-      for (int pp = tid; pp < tsize / 2; pp += NTHREADS) {
-        const int ia = sw<R>(insert0(pp, j)), ib = sw<R>(insert0(pp, j) | (1 << j));
-        C a = tl[ia], b = tl[ib];
-        rot_pair<C, R>(a, b, axis, form, u, (R)-1);
-        tl[ia] = a;
-        tl[ib] = b;
-        if (UNCOMPUTE) {
-          C a2 = tp[ia], b2 = tp[ib];
-          rot_pair<C, R>(a2, b2, axis, form, u, (R)-1);
-          tp[ia] = a2;
-          tp[ib] = b2;
-        }
-      }
-      __syncthreads();
-    }
+    // inverse rotations (they commute, so the group order is free)
+    apply_all<C, R>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S, (R)-1);
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
