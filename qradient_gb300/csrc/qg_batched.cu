@@ -73,37 +73,39 @@ __device__ __forceinline__ double rform(double theta, int* form, double* kappa) 
   return c / s;
 }
 
-// scaled-form rotation of the pair (a: bit 0, b: bit 1); sg = +1 / -1
-template <typename C, typename R>
-__device__ __forceinline__ void rotp(C& a, C& b, int axis, int form, R u, R sg) {
+// scaled-form rotation of the pair (a: bit 0, b: bit 1); SG = +1 / -1 at compile time
+template <int SG, typename C, typename R>
+__device__ __forceinline__ void rotp(C& a, C& b, int axis, int form, R u) {
   const C a0 = a, b0 = b;
+  const R s1 = SG > 0 ? (R)1 : (R)-1;
   if (axis == 0) {
     if (form == 0) {
-      const R us = u * sg;
+      const R us = SG > 0 ? u : -u;
       a.x = fma(us, b0.y, a0.x);
       a.y = fma(-us, b0.x, a0.y);
       b.x = fma(us, a0.y, b0.x);
       b.y = fma(-us, a0.x, b0.y);
     } else {
-      a.x = fma(u, a0.x, sg * b0.y);
-      a.y = fma(u, a0.y, -sg * b0.x);
-      b.x = fma(u, b0.x, sg * a0.y);
-      b.y = fma(u, b0.y, -sg * a0.x);
+      a.x = fma(u, a0.x, SG > 0 ? b0.y : -b0.y);
+      a.y = fma(u, a0.y, SG > 0 ? -b0.x : b0.x);
+      b.x = fma(u, b0.x, SG > 0 ? a0.y : -a0.y);
+      b.y = fma(u, b0.y, SG > 0 ? -a0.x : a0.x);
     }
   } else {
     if (form == 0) {
-      const R us = u * sg;
+      const R us = SG > 0 ? u : -u;
       a.x = fma(-us, b0.x, a0.x);
       a.y = fma(-us, b0.y, a0.y);
       b.x = fma(us, a0.x, b0.x);
       b.y = fma(us, a0.y, b0.y);
     } else {
-      a.x = fma(u, a0.x, -sg * b0.x);
-      a.y = fma(u, a0.y, -sg * b0.y);
-      b.x = fma(u, b0.x, sg * a0.x);
-      b.y = fma(u, b0.y, sg * a0.y);
+      a.x = fma(u, a0.x, SG > 0 ? -b0.x : b0.x);
+      a.y = fma(u, a0.y, SG > 0 ? -b0.y : b0.y);
+      b.x = fma(u, b0.x, SG > 0 ? a0.x : -a0.x);
+      b.y = fma(u, b0.y, SG > 0 ? a0.y : -a0.y);
     }
   }
+  (void)s1;
 }
 
 // reduction term of one pair for Im<lam|P|psi>: X: Im(conj la qb) + Im(conj lb qa);
@@ -123,9 +125,9 @@ __device__ __forceinline__ R wsum(R v) {
 
 // G rotations on ascending local bits bits[0..G-1], each thread owning the
 // 2^G amplitudes of one task (all other bits fixed) in registers.
-template <typename C, typename R, int G, int NT, bool DBL>
+template <typename C, typename R, int G, int NT, bool DBL, int SG>
 __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, const int* axis, const int* form,
-                                          const double* u, R sg) {
+                                          const double* u) {
   const int ntask = M >> G;
   int b[G];
   int ax[G], fm[G];
@@ -161,7 +163,7 @@ __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, c
       for (int i = 0; i < G; ++i)
 #pragma unroll
         for (int c = 0; c < (1 << G); ++c)
-          if (!((c >> i) & 1)) rotp<C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i], sg);
+          if (!((c >> i) & 1)) rotp<SG, C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i]);
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
     }
@@ -429,16 +431,25 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
       __syncthreads();
     };
     // X/Y rotations of the layer in groups of up to 3 bits per shared-memory pass
-    auto rotate = [&](C* v, C* v2, R sg) {
+    auto rotate = [&](C* v, C* v2, bool inverse) {
       const int nxy = S.nxy;
       for (int g0 = 0; g0 < nxy; g0 += 3) {
         const int g = nxy - g0 < 3 ? nxy - g0 : 3;
-        if (g == 3)
-          rot_group<C, R, 3, NT, DBL>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sg);
-        else if (g == 2)
-          rot_group<C, R, 2, NT, DBL>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sg);
-        else
-          rot_group<C, R, 1, NT, DBL>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sg);
+        if (!inverse) {
+          if (g == 3)
+            rot_group<C, R, 3, NT, DBL, 1>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0);
+          else if (g == 2)
+            rot_group<C, R, 2, NT, DBL, 1>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0);
+          else
+            rot_group<C, R, 1, NT, DBL, 1>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0);
+        } else {
+          if (g == 3)
+            rot_group<C, R, 3, NT, DBL, -1>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0);
+          else if (g == 2)
+            rot_group<C, R, 2, NT, DBL, -1>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0);
+          else
+            rot_group<C, R, 1, NT, DBL, -1>(v, v2, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0);
+        }
         __syncthreads();
       }
       if (CS > 1 && S.ncross) {
@@ -452,13 +463,19 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
             const C own = v[swb(e, DBL)];
             const C rem = (v == psi ? rpsi : rlam)[swb(e, DBL)];
             C x0 = rank == 0 ? own : rem, x1 = rank == 0 ? rem : own;
-            rotp<C, R>(x0, x1, S.caxis, S.cform, (R)S.cu, sg);
+            if (inverse)
+              rotp<-1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
+            else
+              rotp<1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
             na[k] = rank == 0 ? x0 : x1;
             if (v2) {
               const C own2 = v2[swb(e, DBL)];
               const C rem2 = (v2 == psi ? rpsi : rlam)[swb(e, DBL)];
               C y0 = rank == 0 ? own2 : rem2, y1 = rank == 0 ? rem2 : own2;
-              rotp<C, R>(y0, y1, S.caxis, S.cform, (R)S.cu, sg);
+              if (inverse)
+                rotp<-1, C, R>(y0, y1, S.caxis, S.cform, (R)S.cu);
+              else
+                rotp<1, C, R>(y0, y1, S.caxis, S.cform, (R)S.cu);
               nb[k] = rank == 0 ? y0 : y1;
             }
           }
@@ -500,7 +517,7 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
       build_diag(i, false);
       apply_diag(psi, false);
       if (CS > 1) cluster.sync();
-      rotate(psi, nullptr, (R)1);
+      rotate(psi, nullptr, false);
       if (J.kind == 0 && J.entangler != 0 && J.placement == 1) entangle(psi, false);
     }
     if (CS > 1) cluster.sync();
@@ -662,7 +679,7 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
         // the partner may still read this CTA's psi for its top-bit reduction
         if (CS > 1) cluster.sync();
         // inverse rotations on lam and psi
-        rotate(lam, psi, (R)-1);
+        rotate(lam, psi, true);
         build_diag(i, true);
         apply_diag(lam, true);
         apply_diag(psi, true);

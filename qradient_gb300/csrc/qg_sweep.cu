@@ -131,37 +131,48 @@ __device__ __forceinline__ double rot_form(double theta, int* form, double* kapp
 }
 
 // Apply one X/Y rotation (scaled form) to the pair (a, b) = (bit 0, bit 1).
-// sg = +1 applies R(theta), sg = -1 applies R(-theta).
-template <typename C, typename R>
-__device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u, R sg) {
+// SG = +1 applies R(theta), SG = -1 applies R(-theta); a compile-time sign,
+// so it folds into the FMAs' operand negations.
+template <int SG, typename C, typename R>
+__device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u) {
   const C a0 = a, b0 = b;
   if (axis == AX_X) {
-    // -i * sg applied to the partner: (-i v) = (v.y, -v.x)
+    // -i * SG applied to the partner: (-i v) = (v.y, -v.x)
     if (form == 0) {
-      const R us = u * sg;
+      const R us = SG > 0 ? u : -u;
       a.x = fma(us, b0.y, a0.x);
       a.y = fma(-us, b0.x, a0.y);
       b.x = fma(us, a0.y, b0.x);
       b.y = fma(-us, a0.x, b0.y);
+    } else if (SG > 0) {
+      a.x = fma(u, a0.x, b0.y);
+      a.y = fma(u, a0.y, -b0.x);
+      b.x = fma(u, b0.x, a0.y);
+      b.y = fma(u, b0.y, -a0.x);
     } else {
-      a.x = fma(u, a0.x, sg * b0.y);
-      a.y = fma(u, a0.y, -sg * b0.x);
-      b.x = fma(u, b0.x, sg * a0.y);
-      b.y = fma(u, b0.y, -sg * a0.x);
+      a.x = fma(u, a0.x, -b0.y);
+      a.y = fma(u, a0.y, b0.x);
+      b.x = fma(u, b0.x, -a0.y);
+      b.y = fma(u, b0.y, a0.x);
     }
   } else {
     // Y: [[1, -t],[t, 1]] (form 0) or [[u, -1],[1, u]] (form 1)
     if (form == 0) {
-      const R us = u * sg;
+      const R us = SG > 0 ? u : -u;
       a.x = fma(-us, b0.x, a0.x);
       a.y = fma(-us, b0.y, a0.y);
       b.x = fma(us, a0.x, b0.x);
       b.y = fma(us, a0.y, b0.y);
+    } else if (SG > 0) {
+      a.x = fma(u, a0.x, -b0.x);
+      a.y = fma(u, a0.y, -b0.y);
+      b.x = fma(u, b0.x, a0.x);
+      b.y = fma(u, b0.y, a0.y);
     } else {
-      a.x = fma(u, a0.x, -sg * b0.x);
-      a.y = fma(u, a0.y, -sg * b0.y);
-      b.x = fma(u, b0.x, sg * a0.x);
-      b.y = fma(u, b0.y, sg * a0.y);
+      a.x = fma(u, a0.x, b0.x);
+      a.y = fma(u, a0.y, b0.y);
+      b.x = fma(u, b0.x, -a0.x);
+      b.y = fma(u, b0.y, -a0.y);
     }
   }
 }
@@ -327,9 +338,9 @@ __device__ __forceinline__ void red_add(SetupShared& S, int slot, R v) {
 // of one task (all other tile bits fixed) in registers: one shared-memory
 // round trip and one barrier per group instead of per rotation.
 
-template <typename C, typename R, int G>
-__device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S, int g0,
-                                            R sg) {
+template <typename C, typename R, int G, int SG>
+__device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S,
+                                            int g0) {
   int b[G], ax[G], fm[G];
   R uu[G];
 #pragma unroll
@@ -364,7 +375,7 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
       for (int i = 0; i < G; ++i)
 #pragma unroll
         for (int c = 0; c < (1 << G); ++c)
-          if (!((c >> i) & 1)) rot_pair<C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i], sg);
+          if (!((c >> i) & 1)) rot_pair<SG, C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i]);
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
     }
@@ -426,16 +437,16 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
   for (int i = 0; i < G; ++i) red_add<R>(S, RS_XY + g0 + i, acc[i]);
 }
 
-template <typename C, typename R>
-__device__ __forceinline__ void apply_all(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S, R sg) {
+template <typename C, typename R, int SG>
+__device__ __forceinline__ void apply_all(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S) {
   for (int g0 = 0; g0 < d.nxy; g0 += 3) {
     const int g = d.nxy - g0 < 3 ? d.nxy - g0 : 3;
     if (g == 3)
-      apply_group<C, R, 3>(v, v2, tsize, d, S, g0, sg);
+      apply_group<C, R, 3, SG>(v, v2, tsize, d, S, g0);
     else if (g == 2)
-      apply_group<C, R, 2>(v, v2, tsize, d, S, g0, sg);
+      apply_group<C, R, 2, SG>(v, v2, tsize, d, S, g0);
     else
-      apply_group<C, R, 1>(v, v2, tsize, d, S, g0, sg);
+      apply_group<C, R, 1, SG>(v, v2, tsize, d, S, g0);
     __syncthreads();
   }
 }
@@ -486,7 +497,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
       }
     }
     __syncthreads();
-    apply_all<C, R>(tile, nullptr, tsize, d, S, (R)1);
+    apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
@@ -602,7 +613,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
     }
     __syncthreads();
     // inverse rotations (they commute, so the group order is free)
-    apply_all<C, R>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S, (R)-1);
+    apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
