@@ -108,6 +108,34 @@ __device__ __forceinline__ void rotp(C& a, C& b, int axis, int form, R u) {
   (void)s1;
 }
 
+template <int SG, int AXIS, int FORM, typename C, typename R>
+__device__ __forceinline__ void rotp_t(C& a, C& b, R u) {
+  rotp<SG, C, R>(a, b, AXIS, FORM, u);
+}
+
+template <int SG, int AXIS, int FORM, int I, int G, typename C, typename R>
+__device__ __forceinline__ void rotb(C* el, R u) {
+#pragma unroll
+  for (int c = 0; c < (1 << G); ++c)
+    if (!((c >> I) & 1)) rotp_t<SG, AXIS, FORM, C, R>(el[c], el[c | (1 << I)], u);
+}
+
+// warp-uniform dispatch around whole unrolled blocks (no predicated variants)
+template <int SG, int I, int G, typename C, typename R>
+__device__ __forceinline__ void rotb_any(C* el, int axis, int form, R u) {
+  if (axis == 0) {
+    if (form == 0)
+      rotb<SG, 0, 0, I, G>(el, u);
+    else
+      rotb<SG, 0, 1, I, G>(el, u);
+  } else {
+    if (form == 0)
+      rotb<SG, 1, 0, I, G>(el, u);
+    else
+      rotb<SG, 1, 1, I, G>(el, u);
+  }
+}
+
 // reduction term of one pair for Im<lam|P|psi>: X: Im(conj la qb) + Im(conj lb qa);
 // Y: -Re(conj la qb) + Re(conj lb qa)
 template <typename C, typename R>
@@ -159,11 +187,9 @@ __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, c
       C el[1 << G];
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) el[c] = w[idx[c]];
-#pragma unroll
-      for (int i = 0; i < G; ++i)
-#pragma unroll
-        for (int c = 0; c < (1 << G); ++c)
-          if (!((c >> i) & 1)) rotp<SG, C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i]);
+      rotb_any<SG, 0, G>(el, ax[0], fm[0], uu[0]);
+      if (G > 1) rotb_any<SG, (G > 1 ? 1 : 0), G>(el, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
+      if (G > 2) rotb_any<SG, (G > 2 ? 2 : 0), G>(el, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
     }

@@ -177,6 +177,64 @@ __device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u) {
   }
 }
 
+// The same rotation with axis and form fixed at compile time (for unrolled
+// register code, where a runtime branch would be if-converted and all four
+// variants issued under predication).
+template <int SG, int AXIS, int FORM, typename C, typename R>
+__device__ __forceinline__ void rot_pair_t(C& a, C& b, R u) {
+  const C a0 = a, b0 = b;
+  const R us = SG > 0 ? u : -u;
+  if (AXIS == AX_X) {
+    if (FORM == 0) {
+      a.x = fma(us, b0.y, a0.x);
+      a.y = fma(-us, b0.x, a0.y);
+      b.x = fma(us, a0.y, b0.x);
+      b.y = fma(-us, a0.x, b0.y);
+    } else {
+      a.x = fma(u, a0.x, SG > 0 ? b0.y : -b0.y);
+      a.y = fma(u, a0.y, SG > 0 ? -b0.x : b0.x);
+      b.x = fma(u, b0.x, SG > 0 ? a0.y : -a0.y);
+      b.y = fma(u, b0.y, SG > 0 ? -a0.x : a0.x);
+    }
+  } else {
+    if (FORM == 0) {
+      a.x = fma(-us, b0.x, a0.x);
+      a.y = fma(-us, b0.y, a0.y);
+      b.x = fma(us, a0.x, b0.x);
+      b.y = fma(us, a0.y, b0.y);
+    } else {
+      a.x = fma(u, a0.x, SG > 0 ? -b0.x : b0.x);
+      a.y = fma(u, a0.y, SG > 0 ? -b0.y : b0.y);
+      b.x = fma(u, b0.x, SG > 0 ? a0.x : -a0.x);
+      b.y = fma(u, b0.y, SG > 0 ? a0.y : -a0.y);
+    }
+  }
+}
+
+// all pairs of register block el[] that differ in bit I, one rotation type
+template <int SG, int AXIS, int FORM, int I, int G, typename C, typename R>
+__device__ __forceinline__ void rot_block(C* el, R u) {
+#pragma unroll
+  for (int c = 0; c < (1 << G); ++c)
+    if (!((c >> I) & 1)) rot_pair_t<SG, AXIS, FORM, C, R>(el[c], el[c | (1 << I)], u);
+}
+
+template <int SG, int I, int G, typename C, typename R>
+__device__ __forceinline__ void rot_block_any(C* el, int axis, int form, R u) {
+  // warp-uniform branch around whole unrolled blocks
+  if (axis == AX_X) {
+    if (form == 0)
+      rot_block<SG, AX_X, 0, I, G>(el, u);
+    else
+      rot_block<SG, AX_X, 1, I, G>(el, u);
+  } else {
+    if (form == 0)
+      rot_block<SG, AX_Y, 0, I, G>(el, u);
+    else
+      rot_block<SG, AX_Y, 1, I, G>(el, u);
+  }
+}
+
 // ------------------------------------------------------------ shared setup
 
 // reduction slots of one CTA: X/Y rotations, U_j of the Z rotations, the
@@ -371,11 +429,9 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
       C el[1 << G];
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) el[c] = w[idx[c]];
-#pragma unroll
-      for (int i = 0; i < G; ++i)
-#pragma unroll
-        for (int c = 0; c < (1 << G); ++c)
-          if (!((c >> i) & 1)) rot_pair<SG, C, R>(el[c], el[c | (1 << i)], ax[i], fm[i], uu[i]);
+      rot_block_any<SG, 0, G>(el, ax[0], fm[0], uu[0]);
+      if (G > 1) rot_block_any<SG, (G > 1 ? 1 : 0), G>(el, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
+      if (G > 2) rot_block_any<SG, (G > 2 ? 2 : 0), G>(el, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
     }
@@ -387,6 +443,22 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
 template <typename C, typename R>
 __device__ __forceinline__ R red_pair(const C& la, const C& lb, const C& qa, const C& qb, int axis, R a) {
   if (axis == AX_X) {
+    a = fma(la.x, qb.y, a);
+    a = fma(-la.y, qb.x, a);
+    a = fma(lb.x, qa.y, a);
+    a = fma(-lb.y, qa.x, a);
+  } else {
+    a = fma(-la.x, qb.x, a);
+    a = fma(-la.y, qb.y, a);
+    a = fma(lb.x, qa.x, a);
+    a = fma(lb.y, qa.y, a);
+  }
+  return a;
+}
+
+template <int AXIS, typename C, typename R>
+__device__ __forceinline__ R red_pair_t(const C& la, const C& lb, const C& qa, const C& qb, R a) {
+  if (AXIS == AX_X) {
     a = fma(la.x, qb.y, a);
     a = fma(-la.y, qb.x, a);
     a = fma(lb.x, qa.y, a);
@@ -428,10 +500,18 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
       qa[c] = tp[sw<R>(x)];
     }
 #pragma unroll
-    for (int i = 0; i < G; ++i)
+    for (int i = 0; i < G; ++i) {
+      // warp-uniform branch around the whole unrolled block
+      if (ax[i] == AX_X) {
 #pragma unroll
-      for (int c = 0; c < (1 << G); ++c)
-        if (!((c >> i) & 1)) acc[i] = red_pair<C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], ax[i], acc[i]);
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] = red_pair_t<AX_X, C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], acc[i]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] = red_pair_t<AX_Y, C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], acc[i]);
+      }
+    }
   }
 #pragma unroll
   for (int i = 0; i < G; ++i) red_add<R>(S, RS_XY + g0 + i, acc[i]);
