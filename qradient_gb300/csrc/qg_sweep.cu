@@ -248,7 +248,8 @@ struct SetupShared {
   double zs[ZMAX], zc[ZMAX];
   double K;  // product of the folded scale factors (diagonal sweeps)
   int form[TMAX];
-  int zk[ZMAX];        // Z rotation on a tile bit walked by the element loop: its k bit, else -1
+  int zk[ZMAX];        // Z rotation bit: k bit of the element loop (>= 0), thread bit (-1), outside (-2)
+  int zkmask;          // k bits carrying a Z rotation
   int64_t offhi[32];   // deposit(k << 8) for the element loop
   uint8_t outside[QMAX];
   double startP[QMAX + 1];
@@ -278,11 +279,23 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
     S.kappa[tid] = k;
   }
   if (tid < d.nz) {
-    // local tile position of the Z rotation's bit
-    int zk = -1;
-    for (int i = 8; i < t; ++i)
-      if (d.bits[i] == d.z[tid].gbit) zk = i - 8;
+    // where the Z rotation's bit lives: tile position >= 8 (a bit of the
+    // element-loop index k, zk = position - 8), a bit of the thread index
+    // (zk = -1), or outside the tile (zk = -2)
+    int zk = -2;
+    for (int i = 0; i < t; ++i)
+      if (d.bits[i] == d.z[tid].gbit) zk = i >= 8 ? i - 8 : -1;
     S.zk[tid] = zk;
+  }
+  if (tid == 0) {
+    int m = 0;
+    for (int j = 0; j < d.nz; ++j) {
+      int zk = -2;
+      for (int i = 8; i < t; ++i)
+        if (d.bits[i] == d.z[j].gbit) zk = i - 8;
+      if (zk >= 0) m |= 1 << zk;
+    }
+    S.zkmask = m;
   }
   for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;
   if (t > 8) {
@@ -380,6 +393,32 @@ __device__ __forceinline__ C apply_diag(C v, uint64_t x, const SweepDesc& d, con
       v = cscale(v, ztab[0].x);
   }
   return v;
+}
+
+// Warp sums of up to three per-thread values at once (transposed butterfly:
+// halves of the values travel at the first two steps), added into this
+// warp's slots slot0, slot0+1, slot0+2: 6 adds per lane instead of 15.
+template <typename R, int G>
+__device__ __forceinline__ void red_add3(SetupShared& S, int slot0, const R* acc) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const R v0 = acc[0], v1 = G > 1 ? acc[1] : (R)0, v2 = G > 2 ? acc[2] : (R)0, v3 = (R)0;
+  const bool h16 = lane & 16, h8 = lane & 8;
+  R k0 = h16 ? v2 : v0, k1 = h16 ? v3 : v1;
+  const R s0 = h16 ? v0 : v2, s1 = h16 ? v1 : v3;
+  k0 += __shfl_xor_sync(full, s0, 16);
+  k1 += __shfl_xor_sync(full, s1, 16);
+  R k = h8 ? k1 : k0;
+  const R s = h8 ? k0 : k1;
+  k += __shfl_xor_sync(full, s, 8);
+  k += __shfl_xor_sync(full, k, 4);
+  k += __shfl_xor_sync(full, k, 2);
+  k += __shfl_xor_sync(full, k, 1);
+  // lanes 0-7: v0, 8-15: v1, 16-23: v2, 24-31: v3
+  const int w = threadIdx.x >> 5;
+  if (lane == 0) S.red[w][slot0] += (double)k;
+  if (G > 1 && lane == 8) S.red[w][slot0 + 1] += (double)k;
+  if (G > 2 && lane == 16) S.red[w][slot0 + 2] += (double)k;
 }
 
 // add a per-thread value into this warp's reduction slot
@@ -513,8 +552,7 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
       }
     }
   }
-#pragma unroll
-  for (int i = 0; i < G; ++i) red_add<R>(S, RS_XY + g0 + i, acc[i]);
+  red_add3<R, G>(S, RS_XY + g0, acc);
 }
 
 template <typename C, typename R, int SG>
@@ -638,12 +676,16 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
     psi_mult = (R)m;
   }
 
+  // Z-rotation sums kept per thread across tiles: the element total T and
+  // U per element-loop bit (tile bits 8..t-1); bits inside the thread index
+  // are resolved at the end, bits outside the tile per tile.
+  double Tacc = 0.0;
+  double Uk[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  bool any_base = false;
+  for (int j = 0; j < d.nz; ++j) any_base |= S.zk[j] == -2;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
     R tT = (R)0, tG = (R)0;
-    R tU[ZMAX];
-#pragma unroll
-    for (int j = 0; j < ZMAX; ++j) tU[j] = (R)0;
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
@@ -657,8 +699,8 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
           const R w = fma(l.x, q.y, -l.y * q.x);  // Im(conj(l) q)
           tT += w;
 #pragma unroll
-          for (int j = 0; j < ZMAX; ++j)
-            if (j < d.nz && S.zk[j] >= 0 && ((k >> S.zk[j]) & 1)) tU[j] += w;
+          for (int i = 0; i < 5; ++i)
+            if (((k >> i) & 1) && (S.zkmask >> i) & 1) Uk[i] += (double)w;
           if (d.gslot >= 0) {
             const R cx = (R)(d.gcost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x]);
             tG = fma(cx, w, tG);
@@ -669,15 +711,15 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       }
     }
     if (d.nz > 0) {
-      const uint64_t x0 = (uint64_t)(base | dep_lo);
-#pragma unroll
-      for (int j = 0; j < ZMAX; ++j) {
-        if (j < d.nz) {
-          const R u = S.zk[j] >= 0 ? tU[j] : (((x0 >> d.z[j].gbit) & 1) && active ? tT : (R)0);
-          red_add<R>(S, RS_Z + j, u);
+      Tacc += (double)tT;
+      if (any_base) {
+        // Z bits outside the tile: the whole tile's total counts when the bit is set
+        const R tot = warp_sum(tT);
+        if ((tid & 31) == 0) {
+          for (int j = 0; j < d.nz; ++j)
+            if (S.zk[j] == -2 && ((base >> d.z[j].gbit) & 1)) S.red[tid >> 5][RS_Z + j] += (double)tot;
         }
       }
-      red_add<R>(S, RS_T, tT);
     }
     if (d.gslot >= 0) red_add<R>(S, RS_G, tG);
     __syncthreads();
@@ -708,6 +750,24 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
     __syncthreads();
   }
 
+  // Z rotations: per-thread sums into the warp slots once per CTA
+  if (d.nz > 0) {
+    for (int j = 0; j < d.nz; ++j) {
+      const int zk = S.zk[j];
+      double v;
+      if (zk >= 0)
+        v = Uk[zk < 5 ? zk : 0];
+      else if (zk == -1)
+        v = (active && ((dep_lo >> d.z[j].gbit) & 1)) ? Tacc : 0.0;  // bit fixed per thread
+      else
+        continue;  // outside the tile: added per tile
+      v = warp_sum(v);
+      if ((tid & 31) == 0) S.red[tid >> 5][RS_Z + j] += v;
+    }
+    const double tt = warp_sum(Tacc);
+    if ((tid & 31) == 0) S.red[tid >> 5][RS_T] += tt;
+  }
+  __syncthreads();
   // CTA totals -> partials[slot][blockIdx]
   if (tid < RS_N) {
     int slot = -1;
