@@ -679,8 +679,8 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   // Z-rotation sums kept per thread across tiles: the element total T and
   // U per element-loop bit (tile bits 8..t-1); bits inside the thread index
   // are resolved at the end, bits outside the tile per tile.
-  double Tacc = 0.0;
-  double Uk[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  R Tacc = (R)0;
+  R Uk[5] = {(R)0, (R)0, (R)0, (R)0, (R)0};
   bool any_base = false;
   for (int j = 0; j < d.nz; ++j) any_base |= S.zk[j] == -2;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
           tT += w;
 #pragma unroll
           for (int i = 0; i < 5; ++i)
-            if (((k >> i) & 1) && (S.zkmask >> i) & 1) Uk[i] += (double)w;
+            if (((k >> i) & 1) && (S.zkmask >> i) & 1) Uk[i] += w;
           if (d.gslot >= 0) {
             const R cx = (R)(d.gcost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x]);
             tG = fma(cx, w, tG);
@@ -711,7 +711,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       }
     }
     if (d.nz > 0) {
-      Tacc += (double)tT;
+      Tacc += tT;
       if (any_base) {
         // Z bits outside the tile: the whole tile's total counts when the bit is set
         const R tot = warp_sum(tT);
@@ -754,18 +754,18 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   if (d.nz > 0) {
     for (int j = 0; j < d.nz; ++j) {
       const int zk = S.zk[j];
-      double v;
+      R v;
       if (zk >= 0)
         v = Uk[zk < 5 ? zk : 0];
       else if (zk == -1)
-        v = (active && ((dep_lo >> d.z[j].gbit) & 1)) ? Tacc : 0.0;  // bit fixed per thread
+        v = (active && ((dep_lo >> d.z[j].gbit) & 1)) ? Tacc : (R)0;  // bit fixed per thread
       else
         continue;  // outside the tile: added per tile
       v = warp_sum(v);
-      if ((tid & 31) == 0) S.red[tid >> 5][RS_Z + j] += v;
+      if ((tid & 31) == 0) S.red[tid >> 5][RS_Z + j] += (double)v;
     }
-    const double tt = warp_sum(Tacc);
-    if ((tid & 31) == 0) S.red[tid >> 5][RS_T] += tt;
+    const R tt = warp_sum(Tacc);
+    if ((tid & 31) == 0) S.red[tid >> 5][RS_T] += (double)tt;
   }
   __syncthreads();
   // CTA totals -> partials[slot][blockIdx]
