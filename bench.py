@@ -138,6 +138,12 @@ def dist_setup():
     return world, rank, local
 
 
+def replica_value(world, ms_per_step):
+    """Whole-job circuits/s of `world` replicas, each one circuit per step,
+    timed by the slowest rank."""
+    return world * 1e3 / ms_per_step
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -500,7 +506,7 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     ms_per_step = ms / args.steps
-    value = world * 1e3 / ms_per_step
+    value = replica_value(world, ms_per_step)
 
     # end to end through the public API: host angles in, host E + grad out
     e2e_s = float("nan")
