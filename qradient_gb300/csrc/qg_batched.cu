@@ -217,7 +217,7 @@ struct BShared {
 }  // namespace
 
 template <typename R, int CS, int NT>
-__global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict__ jobs, int njobs, int* counter,
+__global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restrict__ jobs, int njobs, int* counter,
                                                       int mmax) {
   using C = typename BatchC<R>::T;
   constexpr bool DBL = sizeof(R) == 8;
@@ -225,17 +225,17 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
   __shared__ BShared S;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int Mmax = 1 << mmax;
-  C* psi = (C*)smem;
-  C* lam = psi + Mmax;
-  C* ztab = lam + Mmax;               // BATCH_TABLE entries: Z-rotation phases or QAOA cost phases
+  // three state buffers: psi, lambda and a scratch that permutations and
+  // top-bit rotations write into before the roles are swapped
+  C* const buf0 = (C*)smem;
+  C* ztab = buf0 + 3 * Mmax;          // BATCH_TABLE entries: Z-rotation phases or QAOA cost phases
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = CS > 1 ? (int)cluster.block_rank() : 0;
-  C* rpsi = psi;
-  C* rlam = lam;
-  if (CS > 1) {
-    rpsi = cluster.map_shared_rank(psi, rank ^ 1);
-    rlam = cluster.map_shared_rank(lam, rank ^ 1);
-  }
+  C* psi = buf0;
+  C* lam = buf0 + Mmax;
+  C* scr = buf0 + 2 * Mmax;
+  // the partner CTA's buffer with the same role (same offset)
+  auto remote = [&](C* v) -> C* { return CS > 1 ? cluster.map_shared_rank(v, rank ^ 1) : v; };
   auto csync = [&]() {
     if (CS > 1)
       cluster.sync();
@@ -253,6 +253,9 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
     const int jid = S.job;
     if (jid >= njobs) break;
     const BatchJob J = jobs[jid];
+    psi = buf0;
+    lam = buf0 + Mmax;
+    scr = buf0 + 2 * Mmax;
     const int n = J.n;
     const int m = n - (CS > 1 ? 1 : 0);
     const int M = 1 << m;
@@ -299,86 +302,82 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
     // ---- helpers bound to this job
     // layer setup: rotations of layer i into S (forward coefficients)
     auto setup_layer = [&](int i) {
-      if (tid == 0) {
-        int nxy = 0, nz = 0;
-        S.ncross = 0;
-        for (int q = 0; q < n; ++q) {
-          const int axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
-          const int b = n - 1 - q;
-          const int slot = J.kind == 0 ? i * n + q : 2 * i;
-          if (axis == 2) {
-            S.zbit[nz] = b;
-            S.zslot[nz] = slot;
-            ++nz;
-          } else if (CS > 1 && b == m) {
-            S.ncross = 1;
-            S.caxis = axis;
-            S.cslot = slot;
-          } else {
-            S.xbit[nxy] = b;
-            S.xaxis[nxy] = axis;
-            S.xslot[nxy] = slot;
-            ++nxy;
-          }
+      // warp 0, lane q = qubit q: coefficients in parallel; the X/Y and Z
+      // lists are compacted in ascending bit order (descending q) with
+      // ballots, and K is a shuffle product over the warp
+      if (warp == 0) {
+        const unsigned full = 0xffffffffu;
+        const int q = lane;
+        const bool valid = q < n;
+        int axis = 0;
+        double th = 0.0;
+        if (valid) {
+          axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
+          th = J.kind == 0 ? J.params[i * n + q] : J.params[2 * i];
         }
-        // rotations of a layer commute: order the X/Y ones by bit so that the
-        // groups of three below see ascending bits
-        for (int a = 1; a < nxy; ++a)
-          for (int b = a; b > 0 && S.xbit[b] < S.xbit[b - 1]; --b) {
-            int t0 = S.xbit[b]; S.xbit[b] = S.xbit[b - 1]; S.xbit[b - 1] = t0;
-            t0 = S.xaxis[b]; S.xaxis[b] = S.xaxis[b - 1]; S.xaxis[b - 1] = t0;
-            t0 = S.xslot[b]; S.xslot[b] = S.xslot[b - 1]; S.xslot[b - 1] = t0;
-          }
-        S.nxy = nxy;
-        S.nz = nz;
-      }
-      __syncthreads();
-      // coefficients
-      const double beta = J.kind == 1 ? J.params[2 * i] : 0.0;
-      if (tid < S.nxy) {
-        const int q = n - 1 - S.xbit[tid];
-        const double th = J.kind == 0 ? J.params[i * n + q] : beta;
-        int f;
-        double k;
-        S.xu[tid] = rform(th, &f, &k);
-        S.xform[tid] = f;
-      }
-      if (tid == NT - 1 && S.ncross) {
-        const double th = J.kind == 0 ? J.params[i * n + 0] : beta;
-        int f;
-        double k;
-        S.cu = rform(th, &f, &k);
-        S.cform = f;
-      }
-      if (tid < S.nz) {
-        const int q = n - 1 - S.zbit[tid];
-        sincos(0.5 * J.params[i * n + q], &S.zs[tid], &S.zc[tid]);
-      }
-      if (tid == 32) {
-        // K = product of the X/Y scale factors of the layer
-        double K = 1.0;
-        for (int q = 0; q < n; ++q) {
-          const int axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
-          if (axis == 2) continue;
-          const double th = J.kind == 0 ? J.params[i * n + q] : beta;
-          int f;
-          double k;
-          rform(th, &f, &k);
-          K *= k;
+        const int b = n - 1 - q;
+        const int slot = J.kind == 0 ? i * n + q : 2 * i;
+        const bool isz = valid && axis == 2;
+        const bool iscross = valid && !isz && CS > 1 && b == m;
+        const bool isxy = valid && !isz && !iscross;
+        int f = 0;
+        double k = 1.0, u = 0.0, zs = 0.0, zc = 1.0;
+        if (isxy || iscross) u = rform(th, &f, &k);
+        if (isz) sincos(0.5 * th, &zs, &zc);
+        const unsigned mxy = __ballot_sync(full, isxy), mz = __ballot_sync(full, isz);
+        const unsigned above = q == 31 ? 0u : (full << (q + 1));
+        if (isxy) {
+          const int idx = __popc(mxy & above);
+          S.xbit[idx] = b;
+          S.xaxis[idx] = axis;
+          S.xslot[idx] = slot;
+          S.xu[idx] = u;
+          S.xform[idx] = f;
         }
-        S.K = K;
+        if (isz) {
+          const int idx = __popc(mz & above);
+          S.zbit[idx] = b;
+          S.zslot[idx] = slot;
+          S.zs[idx] = zs;
+          S.zc[idx] = zc;
+        }
+        if (iscross) {
+          S.caxis = axis;
+          S.cslot = slot;
+          S.cu = u;
+          S.cform = f;
+        }
+        double kk = (isxy || iscross) ? k : 1.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) kk *= __shfl_xor_sync(full, kk, o);
+        const unsigned mc = __ballot_sync(full, iscross);
+        if (lane == 0) {
+          S.K = kk;
+          S.nxy = __popc(mxy);
+          S.nz = __popc(mz);
+          S.ncross = mc != 0u;
+        }
       }
       __syncthreads();
     };
-    // diagonal of layer i (Z table * K; QAOA cost phase * K); conj for the inverse
+    // diagonal of layer i (Z table * K; QAOA cost phase * K); conj for the inverse.
+    // The Z table is built by doubling: 2^nz complex multiplies in all.
     auto build_diag = [&](int i, bool inv) {
       const int nzt = S.nz < BZMAX ? S.nz : BZMAX;
       if (J.kind == 0) {
-        for (int pat = tid; pat < (1 << nzt); pat += NT) {
-          double2 ph = make_double2(S.K, 0.0);
-          for (int j = 0; j < nzt; ++j)
-            ph = cmulb(ph, make_double2(S.zc[j], ((pat >> j) & 1) ? S.zs[j] : -S.zs[j]));
-          ztab[pat] = toc<C>(ph.x, inv ? -ph.y : ph.y);
+        if (tid == 0) ztab[0] = toc<C>(S.K, 0.0);
+        __syncthreads();
+        for (int j = 0; j < nzt; ++j) {
+          const int h = 1 << j;
+          // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170); conjugated inverse
+          const C e0 = toc<C>(S.zc[j], inv ? S.zs[j] : -S.zs[j]);
+          const C e1 = toc<C>(S.zc[j], inv ? -S.zs[j] : S.zs[j]);
+          for (int pp = tid; pp < h; pp += NT) {
+            const C v = ztab[pp];
+            ztab[pp + h] = cmulb(v, e1);
+            ztab[pp] = cmulb(v, e0);
+          }
+          __syncthreads();
         }
       } else {
         const double g = J.params[2 * i + 1] * J.cost_w0;
@@ -423,8 +422,9 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
       }
       __syncthreads();
     };
-    // entangler on buffer v: (E v)[y] = v[A^{-1} y] (inverse: v[A y]); CZ sign
-    auto entangle = [&](C* v, bool inv) {
+    // entangler on buffer v: (E v)[y] = v[A^{-1} y] (inverse: v[A y]), gathered
+    // into the scratch buffer whose role then swaps with v; CZ: sign in place
+    auto entangle = [&](C*& v, bool inv) {
       if (J.entangler == 2) {
         for (int e = tid; e < M; e += NT) {
           const uint64_t x = top | (uint64_t)e;
@@ -438,26 +438,19 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
         __syncthreads();
         return;
       }
-      C tmp[BatchC<R>::EPT];
-#pragma unroll
-      for (int k = 0; k < BatchC<R>::EPT; ++k) {
-        const int e = tid + k * NT;
-        if (e < M) {
-          const uint64_t x = top | (uint64_t)e;
-          const uint64_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
-          tmp[k] = v[swb((int)(src & (uint64_t)(M - 1)), DBL)];
-        }
+      for (int e = tid; e < M; e += NT) {
+        const uint64_t x = top | (uint64_t)e;
+        const uint64_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
+        scr[swb(e, DBL)] = v[swb((int)(src & (uint64_t)(M - 1)), DBL)];
       }
       __syncthreads();
-#pragma unroll
-      for (int k = 0; k < BatchC<R>::EPT; ++k) {
-        const int e = tid + k * NT;
-        if (e < M) v[swb(e, DBL)] = tmp[k];
-      }
-      __syncthreads();
+      C* t = v;
+      v = scr;
+      scr = t;
     };
     // X/Y rotations of the layer in groups of up to 3 bits per shared-memory pass
-    auto rotate = [&](C* v, C* v2, bool inverse) {
+    auto rotate = [&](C*& v, C* v2in, bool inverse) {
+      C* v2 = v2in;
       const int nxy = S.nxy;
       for (int g0 = 0; g0 < nxy; g0 += 3) {
         const int g = nxy - g0 < 3 ? nxy - g0 : 3;
@@ -479,45 +472,31 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
         __syncthreads();
       }
       if (CS > 1 && S.ncross) {
-        // rotation on the top bit: the partner amplitude lives in the other CTA
-        cluster.sync();
-        C na[BatchC<R>::EPT], nb[BatchC<R>::EPT];
-#pragma unroll
-        for (int k = 0; k < BatchC<R>::EPT; ++k) {
-          const int e = tid + k * NT;
-          if (e < M) {
-            const C own = v[swb(e, DBL)];
-            const C rem = (v == psi ? rpsi : rlam)[swb(e, DBL)];
+        // rotation on the top bit: the partner amplitude lives in the other
+        // CTA; new values go to the scratch buffer, which then becomes v
+        for (int pass = 0; pass < (v2 ? 2 : 1); ++pass) {
+          C*& w = pass ? v2 : v;
+          cluster.sync();
+          const C* rw = remote(w);
+          for (int e = tid; e < M; e += NT) {
+            const C own = w[swb(e, DBL)];
+            const C rem = rw[swb(e, DBL)];
             C x0 = rank == 0 ? own : rem, x1 = rank == 0 ? rem : own;
             if (inverse)
               rotp<-1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
             else
               rotp<1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
-            na[k] = rank == 0 ? x0 : x1;
-            if (v2) {
-              const C own2 = v2[swb(e, DBL)];
-              const C rem2 = (v2 == psi ? rpsi : rlam)[swb(e, DBL)];
-              C y0 = rank == 0 ? own2 : rem2, y1 = rank == 0 ? rem2 : own2;
-              if (inverse)
-                rotp<-1, C, R>(y0, y1, S.caxis, S.cform, (R)S.cu);
-              else
-                rotp<1, C, R>(y0, y1, S.caxis, S.cform, (R)S.cu);
-              nb[k] = rank == 0 ? y0 : y1;
-            }
+            scr[swb(e, DBL)] = rank == 0 ? x0 : x1;
           }
+          cluster.sync();
+          C* t = w;
+          w = scr;
+          scr = t;
         }
-        cluster.sync();
-#pragma unroll
-        for (int k = 0; k < BatchC<R>::EPT; ++k) {
-          const int e = tid + k * NT;
-          if (e < M) {
-            v[swb(e, DBL)] = na[k];
-            if (v2) v2[swb(e, DBL)] = nb[k];
-          }
-        }
-        cluster.sync();
       }
+      return v2;
     };
+
     // block-sum of one value into the job's output (with 2 CTAs: two atomic
     // adds onto 0, whose result does not depend on their order)
     auto emit1 = [&](R val, int slot, double factor) {
@@ -574,7 +553,7 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
               const uint64_t xp = x ^ b0;
               C u;
               if ((xp >> m) != (x >> m))
-                u = rpsi[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
+                u = remote(psi)[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
               else
                 u = psi[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
               const R w = (R)t.w;
@@ -638,7 +617,7 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
           R a = (R)0;
           for (int e = tid; e < M; e += NT) {
             const C l = lam[swb(e, DBL)];
-            const C qr = rpsi[swb(e, DBL)];
+            const C qr = remote(psi)[swb(e, DBL)];
             // rank 0 holds the bit-0 half (a), rank 1 the bit-1 half (b)
             if (S.caxis == 0)
               a += fma(l.x, qr.y, -l.y * qr.x);
@@ -705,7 +684,7 @@ __global__ void __launch_bounds__(NT) batched_kernel(const BatchJob* __restrict_
         // the partner may still read this CTA's psi for its top-bit reduction
         if (CS > 1) cluster.sync();
         // inverse rotations on lam and psi
-        rotate(lam, psi, true);
+        psi = rotate(lam, psi, true);
         build_diag(i, true);
         apply_diag(lam, true);
         apply_diag(psi, true);
@@ -736,7 +715,7 @@ static cudaError_t launch_one(const BatchJob* jobs, int njobs, int* counter, int
                               int* grid_out) {
   using C = typename BatchC<R>::T;
   constexpr int NT = BATCH_THREADS;
-  const size_t smem = (size_t)(2 * (1 << mmax) + BATCH_TABLE) * sizeof(C);
+  const size_t smem = (size_t)(3 * (1 << mmax) + BATCH_TABLE) * sizeof(C);
   auto kern = batched_kernel<R, CS, NT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
