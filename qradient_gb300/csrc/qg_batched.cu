@@ -196,6 +196,56 @@ __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, c
   }
 }
 
+// Gradient reductions of G rotations on ascending bits from one pass over
+// the 2^G-amplitude tasks (lambda and psi in registers); the warp sums land
+// in out[0..G-1] (this warp's reduction slots).
+template <typename C, typename R, int G, int NT, bool DBL>
+__device__ __forceinline__ void red_group(const C* lam, const C* psi, int M, const int* bits, const int* axis,
+                                          double* out) {
+  int b[G], ax[G];
+  R acc[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    b[i] = bits[i];
+    ax[i] = axis[i];
+    acc[i] = (R)0;
+  }
+  const int ntask = M >> G;
+  for (int tk = threadIdx.x; tk < ntask; tk += NT) {
+    int base = tk;
+#pragma unroll
+    for (int i = 0; i < G; ++i) base = ins0(base, b[i]);
+    C la[1 << G], qa[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      int x = base;
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+        if ((c >> i) & 1) x |= 1 << b[i];
+      la[c] = lam[swb(x, DBL)];
+      qa[c] = psi[swb(x, DBL)];
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      // warp-uniform branch around the whole unrolled block
+      if (ax[i] == 0) {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] += redp<C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], 0);
+      } else {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] += redp<C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], 1);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    const R v = wsum(acc[i]);
+    if ((threadIdx.x & 31) == 0) out[i] = (double)v;
+  }
+}
+
 struct BShared {
   int job;
   int nxy, nz, ncross;       // gates of the current layer
@@ -602,15 +652,14 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         }
         // reductions at the end point of the layer's rotations; per-warp sums in S.red[warp][k]
         const int nxy = S.nxy;
-        for (int gi = 0; gi < nxy; ++gi) {
-          const int j = S.xbit[gi];
-          R a = (R)0;
-          for (int pp = tid; pp < M / 2; pp += NT) {
-            const int ia = swb(ins0(pp, j), DBL), ib = swb(ins0(pp, j) | (1 << j), DBL);
-            a += redp<C, R>(lam[ia], lam[ib], psi[ia], psi[ib], S.xaxis[gi]);
-          }
-          a = wsum(a);
-          if (lane == 0) S.red[warp][gi] = (double)a;
+        for (int g0 = 0; g0 < nxy; g0 += 3) {
+          const int g = nxy - g0 < 3 ? nxy - g0 : 3;
+          if (g == 3)
+            red_group<C, R, 3, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+          else if (g == 2)
+            red_group<C, R, 2, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+          else
+            red_group<C, R, 1, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
         }
         int ns = nxy;
         if (CS > 1 && S.ncross) {
