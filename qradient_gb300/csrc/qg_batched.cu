@@ -28,6 +28,7 @@ namespace {
 
 constexpr int BZMAX = 10;     // Z rotations merged per table (2^BZMAX = BATCH_TABLE entries)
 constexpr int BMAXQ = 26;
+constexpr int BTERMS = 64;    // observable weights staged in shared memory
 
 __device__ __forceinline__ double2 cmulb(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
@@ -46,7 +47,10 @@ __device__ __forceinline__ float2 toc<float2>(double x, double y) {
   return make_float2((float)x, (float)y);
 }
 
-__device__ __forceinline__ int swb(int e, bool dbl) { return dbl ? e ^ (((e >> 3) & 1) * 7) : e ^ (((e >> 4) & 1) * 15); }
+// XOR swizzle of the low index bits with the next ones: 8 (complex128) or 16
+// (complex64) amplitudes per 128-byte row, so tasks that stride over the low
+// bits still spread over all banks
+__device__ __forceinline__ int swb(int e, bool dbl) { return dbl ? e ^ ((e >> 3) & 7) : e ^ ((e >> 4) & 15); }
 __device__ __forceinline__ int ins0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
 
 __device__ __forceinline__ uint64_t lad_fwd(uint64_t x, uint64_t odd, uint64_t even) {
@@ -261,6 +265,7 @@ struct BShared {
   double zs[BMAXQ], zc[BMAXQ];
   double K;
   double startP[BMAXQ + 1];
+  double tw[64];             // observable weights of the current job
   double red[32][BMAXQ + 4];
 };
 
@@ -338,6 +343,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       }
     }
     __syncthreads();
+    for (int k = tid; k < J.nterms && k < BTERMS; k += NT) S.tw[k] = J.terms[k].w;
     // start state
     const R plus = (R)exp2(-0.5 * n);
     for (int e = tid; e < M; e += NT) {
@@ -593,10 +599,11 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           for (int k = 0; k < J.nterms; ++k) {
             const BatchTerm t = J.terms[k];
             const uint64_t b0 = 1ull << (n - 1 - t.q0);
+            const R tw = k < BTERMS ? (R)S.tw[k] : (R)t.w;
             if (t.kind >= 2) {
               bool s = (x & b0) != 0;
               if (t.kind == 3) s ^= (x & (1ull << (n - 1 - t.q1))) != 0;
-              const R w = (R)(s ? -t.w : t.w);
+              const R w = s ? -tw : tw;
               lx = fma(w, v.x, lx);
               ly = fma(w, v.y, ly);
             } else {
@@ -606,7 +613,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
                 u = remote(psi)[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
               else
                 u = psi[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
-              const R w = (R)t.w;
+              const R w = tw;
               if (t.kind == 0) {
                 lx = fma(w, u.x, lx);
                 ly = fma(w, u.y, ly);

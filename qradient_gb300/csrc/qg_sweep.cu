@@ -54,19 +54,19 @@ __device__ __forceinline__ uint64_t ladder_inv(uint64_t x, const LadderMasks& m)
 // CZ on all neighbouring qubit pairs: (-1)^{popcount(x & (x >> 1))}
 __device__ __forceinline__ bool cz_negative(uint64_t x) { return __popcll(x & (x >> 1)) & 1; }
 
-// Shared-memory swizzle: XOR the low bits of an element index with a
-// function of the next bit, so that the 8 (complex128) or 16 (complex64)
-// elements a quarter/half warp touches in a pair loop over bits 0..2 (0..3)
-// land in distinct banks.
+// Shared-memory swizzle: XOR the low 3 (complex128) or 4 (complex64) bits of
+// an element index with the next 3 / 4 bits, so that the 8 or 16 elements a
+// quarter / half warp touches land in distinct banks also when the threads
+// stride over the low bits (gate groups on bits 0..2).
 template <typename R>
 __device__ __forceinline__ int sw(int e);
 template <>
 __device__ __forceinline__ int sw<double>(int e) {
-  return e ^ (((e >> 3) & 1) * 7);
+  return e ^ ((e >> 3) & 7);
 }
 template <>
 __device__ __forceinline__ int sw<float>(int e) {
-  return e ^ (((e >> 4) & 1) * 15);
+  return e ^ ((e >> 4) & 15);
 }
 
 __device__ __forceinline__ int insert0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
