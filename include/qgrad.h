@@ -105,6 +105,17 @@ int qg_run(const qg_circuit* c, int dtype, const double* params_dev, const void*
 int qg_grad(const qg_circuit* c, int dtype, int op, const double* params_dev, const void* ini_state_dev,
             void* workspace_dev, size_t workspace_bytes, double* expec_dev, double* grad_dev, qg_stream stream);
 
+/* Component-sampled adjoint gradient (McClean.grad_run_with_component_sampling,
+ * mc_clean.py:80-115): expec_dev receives the full E = <psi|O|psi>, grad_dev
+ * the gradient of <psi|w_k P_k|psi> for the single observable term
+ * `component` (0-based, in the order the terms were given to
+ * qg_mcclean_create).  The caller draws `component`; the reference draws it
+ * with numpy.random.choice over the normalised weights (mc_clean.py:102).
+ * Same workspace as qg_grad. */
+int qg_grad_component(const qg_circuit* c, int dtype, int op, const double* params_dev, const void* ini_state_dev,
+                      int component, void* workspace_dev, size_t workspace_bytes, double* expec_dev,
+                      double* grad_dev, qg_stream stream);
+
 /* Integer MaxCut / ZZ cost table: table_dev[x] = sum over edges (i, j) of
  * z_i z_j with z = +1 for bit 0 (state.py:280-292 with unit weights).
  * edges: host int32 [nedges, 2]. */
@@ -116,6 +127,33 @@ int qg_maxcut_table(int n, int nedges, const int32_t* edges, int32_t* table_dev,
 int qg_sample_workspace_size(int n, size_t* bytes);
 int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t seed, uint64_t offset,
               void* workspace_dev, size_t workspace_bytes, int64_t* out_dev, qg_stream stream);
+
+/* ---- Optimiser steps on the device.  No reference counterpart as C
+ * functions: they are the parameter updates of qradient/optimization.py
+ * (Adam :151-167, GradientDescent :169-175, RateDecayOnPlateau :177-194),
+ * run on the stream of qg_grad so a training loop never copies parameters,
+ * gradients or costs to the host.  Arrays are device float64 of length
+ * nparams; params are updated in place; history_row_dev (optional, may be
+ * NULL) receives a copy of the updated parameters (the param_history row of
+ * McCleanOpt.step / QaoaOpt.step, optimization.py:90,129).  Every operation
+ * is one IEEE-754 double operation in numpy's order (no fused multiply-add),
+ * so results are bit-identical to the reference's for equal gradients.
+ *
+ * qg_adam_step: iter is the step count including this step (1 first);
+ *   m_dev, v_dev are the first and second moments (zero before step 1).
+ * qg_gd_step: step_size is the already-decayed rate
+ *   (decay_function(step_size, iter) of optimization.py:175).
+ * qg_plateau_step: new_cost_dev points at the step's cost (the expectation
+ *   value qg_grad wrote); state_dev holds 3 doubles {best cost, plateau
+ *   counter, step size}, initialised to {1e10, 0, step_size} as at
+ *   optimization.py:180-183. */
+int qg_adam_step(double* params_dev, const double* grad_dev, double* m_dev, double* v_dev, int nparams, int iter,
+                 double step_size, double beta1, double beta2, double eps, double* history_row_dev, qg_stream stream);
+int qg_gd_step(double* params_dev, const double* grad_dev, int nparams, double step_size, double* history_row_dev,
+               qg_stream stream);
+int qg_plateau_step(double* params_dev, const double* grad_dev, int nparams, const double* new_cost_dev,
+                    double* state_dev, int plateau_length, double decay_rate, double* history_row_dev,
+                    qg_stream stream);
 
 /* ---- Batched persistent execution (no reference counterpart: the
  * reference runs one circuit per Python call).  Many small circuits, each

@@ -29,6 +29,7 @@ SIGNATURES = {
     "qg_workspace_size": (_I, [_P, _I, _I, ctypes.POINTER(_SZ)]),
     "qg_run": (_I, [_P, _I, _P, _P, _P, _SZ, _P, _P, _P]),
     "qg_grad": (_I, [_P, _I, _I, _P, _P, _P, _SZ, _P, _P, _P]),
+    "qg_grad_component": (_I, [_P, _I, _I, _P, _P, _I, _P, _SZ, _P, _P, _P]),
     "qg_maxcut_table": (_I, [_I, _I, _P, _P, _P]),
     "qg_sample_workspace_size": (_I, [_I, ctypes.POINTER(_SZ)]),
     "qg_sample": (_I, [_I, _I, _P, _I64, _U64, _U64, _P, _SZ, _P, _P]),
@@ -38,6 +39,10 @@ SIGNATURES = {
     "qg_batch_workspace_size": (_I, [ctypes.POINTER(_SZ)]),
     "qg_batch_launch": (_I, [_I, _P, _I, _I, _I, _P, _SZ, _P]),
     "qg_grad_noalloc": (_I, [_P, _I, _P, _P, _P, _P, _P]),
+    "qg_adam_step": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                          ctypes.c_double, _P, _P]),
+    "qg_gd_step": (_I, [_P, _P, _I, ctypes.c_double, _P, _P]),
+    "qg_plateau_step": (_I, [_P, _P, _I, _P, _P, _I, ctypes.c_double, _P, _P]),
     "qg_profile_enable": (_I, [_I]),
     "qg_profile_collect": (_I, [_I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I)]),
     "qg_status_string": (ctypes.c_char_p, [_I]),

@@ -150,8 +150,11 @@ class NativeCircuit:
                               stream_handle(device)))
         return e, st
 
-    def grad(self, params, dtype, device, op, ini_state=None, workspace=None, out=None):
-        """Adjoint gradient on device; returns (E tensor[1], grad tensor[nparams])."""
+    def grad(self, params, dtype, device, op, ini_state=None, workspace=None, out=None, component=None):
+        """Adjoint gradient on device; returns (E tensor[1], grad tensor[nparams]).
+
+        component: index of one observable term; the gradient is then that
+        term's (qg_grad_component) while E stays the full expectation."""
         lib = _lib.load()
         p = self.params_tensor(params, device)
         ini = self.state_tensor(ini_state, dtype, device)
@@ -161,8 +164,12 @@ class NativeCircuit:
             g = torch.empty(max(self.nparams, 1), dtype=torch.float64, device=device)
         else:
             e, g = out
-        _lib.check(lib.qg_grad(self._h, dtype, op, ptr(p), ptr(ini), ptr(ws), ws.numel(), ptr(e), ptr(g),
-                               stream_handle(device)))
+        if component is None:
+            _lib.check(lib.qg_grad(self._h, dtype, op, ptr(p), ptr(ini), ptr(ws), ws.numel(), ptr(e), ptr(g),
+                                   stream_handle(device)))
+        else:
+            _lib.check(lib.qg_grad_component(self._h, dtype, op, ptr(p), ptr(ini), int(component), ptr(ws),
+                                             ws.numel(), ptr(e), ptr(g), stream_handle(device)))
         return e, g[: self.nparams]
 
 

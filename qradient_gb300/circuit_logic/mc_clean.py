@@ -2,7 +2,8 @@
 
 Same constructor and methods as ``qradient/circuit_logic/mc_clean.py``:
 ``McClean(qubit_number, observable, layer_number, use_observable_components,
-axes=, angles=)``, ``run_expec_val`` (:27-45) and ``grad_run`` (:47-78).
+axes=, angles=)``, ``run_expec_val`` (:27-45), ``grad_run`` (:47-78) and
+``grad_run_with_component_sampling`` (:80-115).
 Each layer applies the entangler, then one Pauli rotation per qubit with the
 axis ``axes[i, q]`` (0 X, 1 Y, 2 Z) and angle ``angles[i, q]``; the circuit
 starts from Ry(pi/4) on every qubit of |0..0> (or of ``ini_state``).
@@ -101,3 +102,27 @@ class McClean(ParametrizedCircuit):
         op = self._grad_op(nat)
         return nat.grad(self._angles() if angles is None else angles, self._dtype_code, dev, op,
                         ini_state=ini_state, out=out)
+
+    def _sample_component(self):
+        """The term index drawn as at mc_clean.py:102: numpy's global RNG,
+        probabilities w_k / sum(w) (observable.py:75-79)."""
+        obs = self.observable
+        if not obs.store_components:
+            raise AttributeError("component sampling needs McClean(..., use_observable_components=True)")
+        return int(np.random.choice(np.arange(obs.num_components), p=obs.weight_distribution))
+
+    def grad_run_with_component_sampling(self, hide_progbar=True, ini_state=None):
+        """Full E and the gradient of one sampled term w_k P_k (mc_clean.py:80-115)."""
+        k = self._sample_component()
+        nat = self.native()
+        dev = self._device()
+        e, g = nat.grad(self._angles(), self._dtype_code, dev, self._grad_op(nat), ini_state=ini_state, component=k)
+        return float(e.item()), g.reshape(self.lnum, self.qnum).cpu().numpy()
+
+    def grad_run_with_component_sampling_tensors(self, angles=None, ini_state=None, out=None):
+        """Device-side grad_run_with_component_sampling (the component is drawn on the host)."""
+        k = self._sample_component()
+        nat = self.native()
+        dev = self._device()
+        return nat.grad(self._angles() if angles is None else angles, self._dtype_code, dev, self._grad_op(nat),
+                        ini_state=ini_state, out=out, component=k)

@@ -23,6 +23,12 @@ class _Gates:
         self._c = circuit
 
     @property
+    def grad_run_tensors(self, params, ini_state=None, out=None):
+        """Device-side grad_run: params [p, 2] (beta, gamma) as a tensor or
+        array; returns (E tensor[1], grad tensor[2p]) without host copies."""
+        nat = self.native()
+        return nat.grad(params, self._dtype_code, self._device(), self._grad_op(nat), ini_state=ini_state, out=out)
+
     def classical_ham(self):
         return self._c.classical_ham()
 
@@ -71,6 +77,12 @@ class Qaoa(ParametrizedCircuit):
         op = self._grad_op(nat)
         e, g = nat.grad(params, self._dtype_code, self._device(), op, ini_state=ini_state)
         return float(e.item()), g.reshape(self.lnum, 2).cpu().numpy()
+
+    def grad_run_tensors(self, params, ini_state=None, out=None):
+        """Device-side grad_run: params [p, 2] (beta, gamma) as a tensor or
+        array; returns (E tensor[1], grad tensor[2p]) without host copies."""
+        nat = self.native()
+        return nat.grad(params, self._dtype_code, self._device(), self._grad_op(nat), ini_state=ini_state, out=out)
 
     def classical_ham(self):
         """The cost diagonal C(x) as float64 (state.py:261-297)."""

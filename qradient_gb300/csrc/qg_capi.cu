@@ -428,9 +428,11 @@ int build_cost(const qg_circuit* c, char* ws, const WsLayout& W, cudaStream_t st
 }
 
 // Observable passes: lam = O psi (store) and the expectation partial sums.
+// `terms` replaces the circuit's observable (the sampled component of
+// grad_run_with_component_sampling); null means the circuit's own terms.
 template <typename R>
 int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, bool grad, const typename C2T<R>::T* psi,
-                   typename C2T<R>::T* lam, char* ws, cudaStream_t st) {
+                   typename C2T<R>::T* lam, char* ws, cudaStream_t st, const std::vector<Term>* terms = nullptr) {
   const int n = c->n;
   double* partials = (double*)(ws + W.partials);
   const int32_t* ci = (const int32_t*)(ws + W.cost);
@@ -460,7 +462,7 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
   }
   // diagonal terms sorted by weight, then X/Y terms of tile A
   std::vector<Term> diag, xy;
-  for (const auto& tm : c->terms) (tm.kind >= QG_PAULI_Z ? diag : xy).push_back(tm);
+  for (const auto& tm : terms ? *terms : c->terms) (tm.kind >= QG_PAULI_Z ? diag : xy).push_back(tm);
   std::stable_sort(diag.begin(), diag.end(), [](const Term& a, const Term& b) { return a.w < b.w; });
   int es = 0;
   for (size_t s = 0; s < lay.tiles.size(); ++s) {
@@ -555,9 +557,11 @@ int do_run(const qg_circuit* c, const double* params, const void* ini, char* ws,
   return QG_OK;
 }
 
+// component >= 0: the gradient of the single observable term `component`
+// (weight included), with E still the full expectation value.
 template <typename R>
 int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, char* ws, size_t wsb, double* expec,
-            double* grad, cudaStream_t st, int dtype) {
+            double* grad, cudaStream_t st, int dtype, int component = -1) {
   using C = typename C2T<R>::T;
   Program P;
   int s = build_program(c, dtype, ini != nullptr, P);
@@ -576,7 +580,17 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
   C* pbuf[2] = {(C*)(ws + W.psi), W.pingpong && !history ? (C*)(ws + W.psi) + N : nullptr};
   int lc = 0, pc = 0;
   if (!history) pc = fin == pbuf[1] ? 1 : 0;
-  s = run_observable<R>(c, P, W, true, fin, lbuf[lc], ws, st);
+  if (component >= 0) {
+    // lam = w_k P_k psi (mc_clean.py:103-105); its expectation slots are then
+    // overwritten by the full-observable pass, which writes at least the
+    // same slots, so E stays <psi|O|psi> (mc_clean.py:99-100)
+    const std::vector<Term> one(1, c->terms[component]);
+    s = run_observable<R>(c, P, W, true, fin, lbuf[lc], ws, st, &one);
+    if (s) return s;
+    s = run_observable<R>(c, P, W, false, fin, nullptr, ws, st);
+  } else {
+    s = run_observable<R>(c, P, W, true, fin, lbuf[lc], ws, st);
+  }
   if (s) return s;
   SweepPtrs<R> p;
   memset(&p, 0, sizeof p);
@@ -841,6 +855,24 @@ int qg_grad(const qg_circuit* c, int dtype, int op, const double* params, const 
   cudaStream_t st = (cudaStream_t)stream;
   if (dtype == QG_C128) return do_grad<double>(c, op, params, ini, (char*)ws, wsb, expec, grad, st, dtype);
   if (dtype == QG_C64) return do_grad<float>(c, op, params, ini, (char*)ws, wsb, expec, grad, st, dtype);
+  return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+}
+
+int qg_grad_component(const qg_circuit* c, int dtype, int op, const double* params, const void* ini, int component,
+                      void* ws, size_t wsb, double* expec, double* grad, qg_stream stream) {
+  if (int s = check_circuit(c)) return s;
+  if (c->kind != 0) return fail(QG_ERR_INVALID, "component sampling is defined for McClean circuits");
+  if (component < 0 || component >= (int)c->terms.size())
+    return fail(QG_ERR_INVALID, "component %d outside 0..%d", component, (int)c->terms.size() - 1);
+  int np = 0;
+  qg_num_params(c, &np);
+  if (np > 0 && (!params || !grad)) return fail(QG_ERR_INVALID, "null params or grad");
+  if (!ws || !expec) return fail(QG_ERR_INVALID, "null workspace or output");
+  if (op != QG_OP_GRAD_HISTORY && op != QG_OP_GRAD_UNCOMPUTE) return fail(QG_ERR_INVALID, "unknown grad op %d", op);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == QG_C128)
+    return do_grad<double>(c, op, params, ini, (char*)ws, wsb, expec, grad, st, dtype, component);
+  if (dtype == QG_C64) return do_grad<float>(c, op, params, ini, (char*)ws, wsb, expec, grad, st, dtype, component);
   return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
 }
 

@@ -8,9 +8,16 @@ the snapshot lacks.  Inputs are seeded (``numpy.random.default_rng``) and
 stored beside the outputs, so the tests never need the reference.
 
 Usage:  python tests/golden/make_golden.py [--reference PATH] [--big]
+        python tests/golden/make_golden.py --optimizer [--reference PATH]
 
 ``--big`` adds the McClean ZZ-chain cases at n = 18, 20 (L = 50), which take
 about two minutes of reference time.
+
+``--optimizer`` writes ``optimizer.npz`` instead: the reference's own
+optimiser classes (``qradient/optimization.py``) fed seeded gradient and cost
+sequences (the update rules alone), and ``McCleanOpt`` / ``QaoaOpt``
+training runs with Adam, GradientDescent and RateDecayOnPlateau (the
+histories of whole training loops).
 """
 import argparse
 import importlib.util
@@ -113,11 +120,157 @@ def qaoa_cases():
     return cases
 
 
+def gd_decay(step_size, it):
+    """Decay function of the GradientDescent golden cases (also in the tests)."""
+    return step_size / (1.0 + 0.25 * it)
+
+
+OPT_RULE_CASES = [
+    # (name, optimizer dict, nparams, steps)
+    ("adam_default", {"name": "Adam"}, 37, 30),
+    ("adam_custom", {"name": "Adam", "step_size": 0.05, "beta1": 0.8, "beta2": 0.99, "eps": 1e-6}, 300, 25),
+    ("gd_plain", {"name": "GradientDescent", "step_size": 0.1}, 37, 20),
+    ("gd_decay", {"name": "GradientDescent", "step_size": 0.2, "decay_function": gd_decay}, 37, 20),
+    ("plateau", {"name": "RateDecayOnPlateau", "step_size": 0.3, "plateau_length": 3, "decay_rate": 0.5}, 37, 40),
+]
+
+COMPONENT_CASES = [
+    # (name, n, L, seed, draws): Pauli-sum observable with positive weights
+    ("comp_n5_L3", 5, 3, 51, 6),
+    ("comp_n7_L4", 7, 4, 52, 6),
+]
+
+
+def component_observable(n, seed):
+    r = np.random.default_rng(seed + 2000)
+    obs = {}
+    for key in ("x", "y", "z"):
+        arr = np.full(n, None)
+        for q in r.choice(n, size=max(1, n // 2), replace=False):
+            arr[q] = float(r.uniform(0.2, 1.0))
+        obs[key] = arr
+    obs["zz"] = zz_pairs(n, [(i, i + 1) for i in range(n - 1)], 0.7)
+    return obs
+
+
+OPT_RUN_CASES = [
+    # (name, family, n, layers, optimizer dict, steps, seed)
+    ("mcclean_adam_n6_L4", "mcclean", 6, 4, {"name": "Adam", "step_size": 0.05}, 15, 41),
+    ("mcclean_gd_n5_L3", "mcclean", 5, 3, {"name": "GradientDescent", "step_size": 0.1,
+                                           "decay_function": gd_decay}, 12, 42),
+    ("mcclean_plateau_n6_L3", "mcclean", 6, 3, {"name": "RateDecayOnPlateau", "step_size": 0.9,
+                                                "plateau_length": 2, "decay_rate": 0.5}, 20, 43),
+    ("qaoa_adam_n8_p3", "qaoa", 8, 3, {"name": "Adam", "step_size": 0.05}, 15, 44),
+    ("mcclean_adam_comp_n6_L3", "mcclean_comp", 6, 3, {"name": "Adam", "step_size": 0.05}, 12, 45),
+]
+
+
+def record(circuit, method):
+    """Keep every gradient the optimiser's steps receive from `method`."""
+    inner = getattr(circuit, method)
+    circuit.recorded_grads = []
+
+    def wrapped(*a, **k):
+        e, g = inner(*a, **k)
+        circuit.recorded_grads.append(np.array(g, dtype=np.float64))
+        return e, g
+
+    setattr(circuit, method, wrapped)
+
+
+def optimizer_main(reference):
+    McClean, Qaoa = load_reference(reference)
+    from qradient import optimization as ropt
+
+    out = {}
+    for name, spec, npar, steps in OPT_RULE_CASES:
+        rng = np.random.default_rng(len(name) * 101 + npar)
+        p0 = rng.uniform(0, 2 * np.pi, npar)
+        grads = rng.normal(size=(steps, npar)) * rng.uniform(1e-3, 2.0, (steps, 1))
+        # costs that fall, then rise for a while, so the plateau rule decays the rate
+        costs = np.cumsum(rng.normal(size=steps) + np.where(np.arange(steps) % 9 < 4, -0.5, 0.4))
+        holder = ropt.ParametrizedCircuitOptimizer()
+        holder.pick(spec, p0.copy())
+        opt = holder.optimizer
+        hist = np.zeros((steps + 1, npar))
+        hist[0] = p0
+        rates = np.zeros(steps)
+        for k in range(steps):
+            opt.step(grads[k], costs[k])
+            hist[k + 1] = opt.parameters
+            rates[k] = opt.step_size
+        key = "rule/" + name + "/"
+        out.update({key + "p0": p0, key + "grads": grads, key + "costs": costs, key + "hist": hist,
+                    key + "rates": rates})
+        print("rule   %-24s done" % name, flush=True)
+
+    for name, n, L, seed, draws in COMPONENT_CASES:
+        rng = np.random.default_rng(seed)
+        obs = component_observable(n, seed)
+        axes = rng.integers(0, 3, (L, n))
+        angles = rng.uniform(0, 2 * np.pi, (L, n))
+        c = McClean(n, obs, L, use_observable_components=True, axes=axes, angles=angles)
+        np.random.seed(seed)
+        es, gs = [], []
+        for _ in range(draws):
+            e, g = c.grad_run_with_component_sampling()
+            es.append(e)
+            gs.append(g.copy())
+        kind, q0, q1, w = obs_to_arrays(n, obs)
+        key = "comp/" + name + "/"
+        out.update({key + "axes": axes.astype(np.int8), key + "angles": angles, key + "kind": kind, key + "q0": q0,
+                    key + "q1": q1, key + "w": w, key + "e": np.array(es), key + "grads": np.array(gs)})
+        print("comp   %-24s done" % name, flush=True)
+
+    for name, fam, n, layers, spec, steps, seed in OPT_RUN_CASES:
+        rng = np.random.default_rng(seed)
+        key = "run/" + name + "/"
+        t0 = time.time()
+        if fam in ("mcclean", "mcclean_comp"):
+            comp = fam == "mcclean_comp"
+            if comp:
+                obs = component_observable(n, seed)
+            else:
+                obs = {"zz": zz_pairs(n, [(i, i + 1) for i in range(n - 1)]),
+                       "x": np.array([0.5] + [None] * (n - 1), dtype=object)}
+            axes = rng.integers(0, 3, (layers, n))
+            angles = rng.uniform(0, 2 * np.pi, (layers, n))
+            c = McClean(n, obs, layers, use_observable_components=comp, axes=axes, angles=angles.copy())
+            record(c, "grad_run_with_component_sampling" if comp else "grad_run")
+            o = ropt.McCleanOpt(c, spec, max_iter=steps + 1)
+            np.random.seed(seed)
+            for _ in range(steps):
+                o.step(component_sampling=comp)
+            out.update({key + "axes": axes.astype(np.int8), key + "angles": angles})
+        else:
+            edges = regular3(n, seed)
+            obs = {"zz": zz_pairs(n, edges)}
+            betas = rng.uniform(0, np.pi, layers)
+            gammas = rng.uniform(0, np.pi, layers)
+            c = Qaoa(n, obs, layers)
+            record(c, "grad_run")
+            o = ropt.QaoaOpt(c, spec, betas, gammas, max_iter=steps + 1)
+            for _ in range(steps):
+                o.step()
+            out.update({key + "edges": np.array(edges, np.int32), key + "betas": betas, key + "gammas": gammas})
+        kind, q0, q1, w = obs_to_arrays(n, obs)
+        out.update({key + "kind": kind, key + "q0": q0, key + "q1": q1, key + "w": w,
+                    key + "param_history": o.param_history, key + "cost_history": o.cost_history,
+                    key + "grads": np.array(c.recorded_grads)})
+        print("run    %-24s %.2fs" % (name, time.time() - t0), flush=True)
+
+    np.savez_compressed(os.path.join(HERE, "optimizer.npz"), **out)
+    print("wrote", len(out), "arrays to optimizer.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--big", action="store_true")
+    ap.add_argument("--optimizer", action="store_true")
     args = ap.parse_args()
+    if args.optimizer:
+        return optimizer_main(args.reference)
     McClean, Qaoa = load_reference(args.reference)
 
     out = {}

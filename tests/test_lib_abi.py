@@ -106,3 +106,27 @@ def test_product_path_fails_loudly_without_gpu():
     c = McClean(3, {"zz": zz}, 1)
     with pytest.raises(RuntimeError, match="CUDA"):
         c.grad_run()
+
+
+def test_optimiser_steps_and_component_gradient_validate_arguments():
+    """Argument checks that return before any CUDA call."""
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    P = ctypes.c_void_p
+    fake = P(256)  # never dereferenced: every call below returns before a launch
+    INV = _lib.QG_ERR_INVALID
+    assert lib.qg_adam_step(fake, fake, fake, fake, -1, 1, 0.1, 0.9, 0.999, 1e-8, None, None) == INV
+    assert lib.qg_adam_step(fake, fake, fake, fake, 4, 0, 0.1, 0.9, 0.999, 1e-8, None, None) == INV
+    assert lib.qg_adam_step(fake, None, fake, fake, 4, 1, 0.1, 0.9, 0.999, 1e-8, None, None) == INV
+    assert lib.qg_adam_step(None, None, None, None, 0, 1, 0.1, 0.9, 0.999, 1e-8, None, None) == 0
+    assert lib.qg_gd_step(fake, fake, -2, 0.1, None, None) == INV
+    assert lib.qg_gd_step(None, fake, 3, 0.1, None, None) == INV
+    assert lib.qg_gd_step(None, None, 0, 0.1, None, None) == 0
+    assert lib.qg_plateau_step(fake, fake, 3, None, fake, 2, 0.5, None, None) == INV
+    st, h = _create(4, 2, np.zeros((2, 4)), kind=(0, 3), q0=(1, 0), q1=(1, 1), w=(0.5, 1.0))
+    assert st == 0
+    for k in (-1, 2):
+        assert lib.qg_grad_component(h, 0, 1, fake, None, k, fake, 1 << 20, fake, fake, None) == INV
+        assert b"component" in lib.qg_last_error()
+    lib.qg_destroy(h)
