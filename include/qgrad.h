@@ -128,6 +128,30 @@ int qg_sample_workspace_size(int n, size_t* bytes);
 int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t seed, uint64_t offset,
               void* workspace_dev, size_t workspace_bytes, int64_t* out_dev, qg_stream stream);
 
+/* ---- Finite-shot estimates (the projector estimator of
+ * ParametrizedCircuit.sample_expec_val / sample_component_expec_val,
+ * base.py:22-46, with the projectors of observable.py:82-177).
+ *
+ * qg_pauli_expectations: out_dev[k] = <psi|P_k|psi> (unweighted, real) for
+ *   every observable term of circuit c, in the order given at creation,
+ *   for a device state of 2^n amplitudes at `dtype`.  Deterministic.
+ *   Workspace: qg_pauli_workspace_size bytes.
+ * qg_projector_shots: for each row r and term k, draws `shots` outcomes of
+ *   the term's +1/-1 projective measurement, +w_k with probability
+ *   p = (1 + <P_k>) / 2 (the reference's ||Pi_+ psi||^2) and -w_k otherwise,
+ *   and writes their mean to term_est_dev[r][k] (optional) and the sum over
+ *   terms to total_dev[r] (optional): the reference's
+ *   sample_expec_val(shots) per row.  expec_dev [nrows][nterms] holds the
+ *   <P_k>, weights_dev [nterms] the w_k.  Uniforms come from
+ *   Philox4x32-10 with key `seed` and counter {offset + r*nterms + k,
+ *   shot / 2}; the reference draws with scipy.stats.rv_discrete instead, so
+ *   parity is statistical.  nterms <= 1024. */
+int qg_pauli_workspace_size(const qg_circuit* c, size_t* bytes);
+int qg_pauli_expectations(const qg_circuit* c, int dtype, const void* state_dev, void* workspace_dev,
+                          size_t workspace_bytes, double* out_dev, qg_stream stream);
+int qg_projector_shots(int nrows, int nterms, const double* expec_dev, const double* weights_dev, int shots,
+                       uint64_t seed, uint64_t offset, double* term_est_dev, double* total_dev, qg_stream stream);
+
 /* ---- Optimiser steps on the device.  No reference counterpart as C
  * functions: they are the parameter updates of qradient/optimization.py
  * (Adam :151-167, GradientDescent :169-175, RateDecayOnPlateau :177-194),

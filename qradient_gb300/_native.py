@@ -150,6 +150,29 @@ class NativeCircuit:
                               stream_handle(device)))
         return e, st
 
+    def run_into(self, params, dtype, device, ini, workspace, expec, state):
+        """qg_run with caller tensors: params and ini already on the device,
+        expec a 1-element float64 view, state a 2^n buffer (or None)."""
+        _lib.check(_lib.load().qg_run(self._h, dtype, ptr(params), ptr(ini), ptr(workspace), workspace.numel(),
+                                      ptr(expec), ptr(state), stream_handle(device)))
+
+    def pauli_workspace(self, device):
+        key = ("pauli", str(device))
+        b = ctypes.c_size_t(0)
+        _lib.check(_lib.load().qg_pauli_workspace_size(self._h, ctypes.byref(b)))
+        ws = self._ws.get(key)
+        if ws is None or ws.numel() < b.value:
+            ws = torch.empty(max(b.value, 8), dtype=torch.uint8, device=device)
+            self._ws[key] = ws
+        return ws
+
+    def pauli_expectations_into(self, state, dtype, device, out):
+        """out[k] = <state|P_k|state> for every observable term (qg_pauli_expectations)."""
+        ws = self.pauli_workspace(device)
+        _lib.check(_lib.load().qg_pauli_expectations(self._h, dtype, ptr(state), ptr(ws), ws.numel(), ptr(out),
+                                                     stream_handle(device)))
+        return out
+
     def grad(self, params, dtype, device, op, ini_state=None, workspace=None, out=None, component=None):
         """Adjoint gradient on device; returns (E tensor[1], grad tensor[nparams]).
 
@@ -171,6 +194,13 @@ class NativeCircuit:
             _lib.check(lib.qg_grad_component(self._h, dtype, op, ptr(p), ptr(ini), int(component), ptr(ws),
                                              ws.numel(), ptr(e), ptr(g), stream_handle(device)))
         return e, g[: self.nparams]
+
+
+def projector_shots(expec, weights, shot_num, seed, offset=0, term_est=None, total=None):
+    """qg_projector_shots over rows of expectations [rows, K] (device)."""
+    rows, K = expec.shape
+    _lib.check(_lib.load().qg_projector_shots(rows, K, ptr(expec), ptr(weights), int(shot_num), int(seed), int(offset),
+                                              ptr(term_est), ptr(total), stream_handle(expec.device)))
 
 
 def choose_grad_op(circuit, dtype, device, mode="auto", budget_fraction=0.6):

@@ -2,8 +2,9 @@
 
 Same constructor and methods as ``qradient/circuit_logic/mc_clean.py``:
 ``McClean(qubit_number, observable, layer_number, use_observable_components,
-axes=, angles=)``, ``run_expec_val`` (:27-45), ``grad_run`` (:47-78) and
-``grad_run_with_component_sampling`` (:80-115).
+axes=, angles=)``, ``run_expec_val`` (:27-45), ``grad_run`` (:47-78),
+``grad_run_with_component_sampling`` (:80-115) and the parameter-shift
+``sample_grad`` / ``sample_grad_with_component_sampling`` (:117-205).
 Each layer applies the entangler, then one Pauli rotation per qubit with the
 axis ``axes[i, q]`` (0 X, 1 Y, 2 Z) and angle ``angles[i, q]``; the circuit
 starts from Ry(pi/4) on every qubit of |0..0> (or of ``ini_state``).
@@ -15,6 +16,7 @@ Extra keyword arguments (not in the reference):
   dtype, device, grad_mode  see ParametrizedCircuit
 """
 import numpy as np
+import torch
 
 from .. import _lib, _native
 from .base import ParametrizedCircuit
@@ -78,13 +80,14 @@ class McClean(ParametrizedCircuit):
 
     # ------------------------------------------------------------ reference API
     def run_expec_val(self, hide_progbar=True, exact_expec_val=True, shot_num=1, ini_state=None):
-        """Run the circuit and return <psi|O|psi> (mc_clean.py:27-45)."""
-        if not exact_expec_val:
-            return self.sample_expec_val(shot_num)
+        """Run the circuit and return <psi|O|psi> (mc_clean.py:27-45), or its
+        projector-shot estimate when exact_expec_val is False."""
         nat = self.native()
         dev = self._device()
         e, st = nat.run(self._angles(), self._dtype_code, dev, ini_state=ini_state, want_state=True)
         self.state.tensor = st
+        if not exact_expec_val:
+            return self.sample_expec_val(shot_num)
         return float(e.item())
 
     def grad_run(self, hide_progbar=True, ini_state=None):
@@ -126,3 +129,73 @@ class McClean(ParametrizedCircuit):
         dev = self._device()
         return nat.grad(self._angles() if angles is None else angles, self._dtype_code, dev, self._grad_op(nat),
                         ini_state=ini_state, out=out, component=k)
+
+    # ------------------------------------------------------------ parameter shift
+    def sample_grad(self, hide_progbar=True, shot_num=1, exact_expec_val=True, ini_state=None, seed=None):
+        """Parameter-shift gradient with projector shots (mc_clean.py:117-156).
+
+        grad[i, q] = (o+ - o-) / 2 with o+- the shot estimate of <O> after
+        rotating qubit q of layer i by a further +-pi/2.  All rotations of a
+        layer commute, so that state is the full circuit with angle
+        angles[i, q] +- pi/2; the 2 L n shifted circuits run as forward
+        passes on the device, each followed by one per-term expectation
+        reduction, and one projector-shot launch draws every estimate.
+        shot_num=None gives the exact parameter-shift gradient (infinitely
+        many shots).  Shots are Philox draws keyed by `seed` (default: drawn
+        from numpy's global RNG)."""
+        return self._shift_grad(shot_num, exact_expec_val, ini_state, seed, False)
+
+    def sample_grad_with_component_sampling(self, hide_progbar=True, shot_num=1, exact_expec_val=True,
+                                            ini_state=None, seed=None):
+        """sample_grad with one observable term per (layer, qubit), drawn
+        with numpy.random.choice over w_k / sum(w) as mc_clean.py:187, and
+        o+- the shot estimate of that term w_k P_k alone (:195-202)."""
+        return self._shift_grad(shot_num, exact_expec_val, ini_state, seed, True)
+
+    def _shift_grad(self, shot_num, exact_expec_val, ini_state, seed, component_sampling):
+        if shot_num is not None:
+            shot_num = self._check_shots(shot_num)
+        nat = self.native()
+        dev = self._device()
+        dt = self._dtype_code
+        L, n = self.lnum, self.qnum
+        K = self.observable.num_components
+        # forward run: E (exact or sampled) and the final state
+        expec_val = self.run_expec_val(exact_expec_val=exact_expec_val, shot_num=shot_num or 1, ini_state=ini_state)
+        comps = [self._sample_component() for _ in range(L * n)] if component_sampling else None
+        base = torch.as_tensor(self._angles(), dtype=torch.float64).reshape(-1).to(dev)
+        rows = 2 * L * n
+        if rows == 0:
+            return expec_val, np.zeros((L, n))
+        shifted = base.repeat(rows, 1)
+        idx = torch.arange(L * n, device=dev)
+        shifted[2 * idx, idx] += np.pi / 2
+        shifted[2 * idx + 1, idx] -= np.pi / 2
+        ini = nat.state_tensor(ini_state, dt, dev)
+        ws = nat.workspace(dt, _lib.QG_OP_RUN, dev)
+        energies = torch.empty(rows, dtype=torch.float64, device=dev)
+        state = torch.empty(2 ** n, dtype=_native.torch_dtype(dt), device=dev)
+        expec = torch.empty((rows, max(K, 1)), dtype=torch.float64, device=dev)
+        need_terms = shot_num is not None or component_sampling
+        for r in range(rows):
+            nat.run_into(shifted[r], dt, dev, ini, ws, energies[r:r + 1], state if need_terms else None)
+            if need_terms and K:
+                nat.pauli_expectations_into(state, dt, dev, expec[r])
+        w = self._weights(dev)
+        if component_sampling:
+            k = torch.as_tensor(np.repeat(comps, 2), device=dev)
+            r_idx = torch.arange(rows, device=dev)
+            if shot_num is None:
+                vals = w[k] * expec[r_idx, k]
+            else:
+                term_est = torch.empty((rows, K), dtype=torch.float64, device=dev)
+                _native.projector_shots(expec[:, :K], w, shot_num, self._shot_seed(seed), term_est=term_est)
+                vals = term_est[r_idx, k]
+        elif shot_num is None:
+            vals = energies
+        else:
+            vals = torch.empty(rows, dtype=torch.float64, device=dev)
+            _native.projector_shots(expec[:, :K], w, shot_num, self._shot_seed(seed), total=vals)
+        v = vals.reshape(L * n, 2)
+        grad = (0.5 * (v[:, 0] - v[:, 1])).reshape(L, n)
+        return expec_val, grad.cpu().numpy()

@@ -23,6 +23,12 @@ class _Gates:
         self._c = circuit
 
     @property
+    def sample_grad(self, betas, gammas, shot_num=1, hide_progbar=True, exact_expec_val=True, ini_state=None):
+        """A stub in the reference too (qaoa.py:72-81): warns and returns None."""
+        import warnings
+
+        warnings.warn("Not implemented yet.")
+
     def grad_run_tensors(self, params, ini_state=None, out=None):
         """Device-side grad_run: params [p, 2] (beta, gamma) as a tensor or
         array; returns (E tensor[1], grad tensor[2p]) without host copies."""
@@ -63,11 +69,11 @@ class Qaoa(ParametrizedCircuit):
     def run_expec_val(self, betas, gammas, hide_progbar=True, exact_expec_val=True, shot_num=1, ini_state=None):
         """Forward run and <psi|O|psi> (qaoa.py:23-38)."""
         params = self.__check_parameters(betas, gammas)
-        if not exact_expec_val:
-            return self.sample_expec_val(shot_num)
         nat = self.native()
         e, st = nat.run(params, self._dtype_code, self._device(), ini_state=ini_state, want_state=True)
         self.state.tensor = st
+        if not exact_expec_val:
+            return self.sample_expec_val(shot_num)
         return float(e.item())
 
     def grad_run(self, betas, gammas, hide_progbar=True, ini_state=None):
@@ -77,6 +83,12 @@ class Qaoa(ParametrizedCircuit):
         op = self._grad_op(nat)
         e, g = nat.grad(params, self._dtype_code, self._device(), op, ini_state=ini_state)
         return float(e.item()), g.reshape(self.lnum, 2).cpu().numpy()
+
+    def sample_grad(self, betas, gammas, shot_num=1, hide_progbar=True, exact_expec_val=True, ini_state=None):
+        """A stub in the reference too (qaoa.py:72-81): warns and returns None."""
+        import warnings
+
+        warnings.warn("Not implemented yet.")
 
     def grad_run_tensors(self, params, ini_state=None, out=None):
         """Device-side grad_run: params [p, 2] (beta, gamma) as a tensor or

@@ -26,6 +26,7 @@
 #include "qg_extra.h"
 #include "qg_internal.cuh"
 #include "qg_kernels.h"
+#include "qg_shots.h"
 
 using namespace qg;
 
@@ -917,6 +918,39 @@ int qg_sample(int n, int dtype, const void* state, int64_t nshots, uint64_t seed
     QG_CUDA(launch_sample<double2>(n, (const double2*)state, nshots, seed, offset, (double*)ws, out, st));
   else if (dtype == QG_C64)
     QG_CUDA(launch_sample<float2>(n, (const float2*)state, nshots, seed, offset, (double*)ws, out, st));
+  else
+    return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+  return QG_OK;
+}
+
+int qg_pauli_workspace_size(const qg_circuit* c, size_t* bytes) {
+  if (int s = check_circuit(c)) return s;
+  if (!bytes) return fail(QG_ERR_INVALID, "null output");
+  *bytes = pauli_workspace_bytes((int)c->terms.size());
+  return QG_OK;
+}
+
+int qg_pauli_expectations(const qg_circuit* c, int dtype, const void* state, void* ws, size_t wsb, double* out,
+                          qg_stream stream) {
+  if (int s = check_circuit(c)) return s;
+  const int K = (int)c->terms.size();
+  if (K == 0) return QG_OK;
+  if (!state || !ws || !out) return fail(QG_ERR_INVALID, "null pointer");
+  const size_t need = pauli_workspace_bytes(K);
+  if (wsb < need) return fail(QG_ERR_WORKSPACE, "workspace %zu bytes < %zu needed", wsb, need);
+  std::vector<PauliTerm> t(K);
+  for (int k = 0; k < K; ++k) {
+    const Term& tm = c->terms[k];
+    t[k].kind = (int8_t)tm.kind;
+    t[k].b0 = (int8_t)(c->n - 1 - tm.q0);
+    t[k].b1 = (int8_t)(tm.kind == QG_PAULI_ZZ ? c->n - 1 - tm.q1 : 0);
+    t[k].pad = 0;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == QG_C128)
+    QG_CUDA(launch_pauli_expectations<double2>(c->n, (const double2*)state, K, t.data(), (double*)ws, out, st));
+  else if (dtype == QG_C64)
+    QG_CUDA(launch_pauli_expectations<float2>(c->n, (const float2*)state, K, t.data(), (double*)ws, out, st));
   else
     return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
   return QG_OK;

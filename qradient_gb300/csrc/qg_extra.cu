@@ -2,6 +2,7 @@
 #include <stdint.h>
 
 #include "qg_extra.h"
+#include "qg_philox.cuh"
 
 namespace qg {
 
@@ -108,37 +109,6 @@ __global__ void scan_kernel(const double* sums, int64_t nb, double* prefix) {
     prefix[i] = run;
     run += sums[i];
   }
-}
-
-struct Philox {
-  uint32_t c[4];
-};
-
-__device__ __forceinline__ void philox_round(uint32_t* c, uint32_t k0, uint32_t k1) {
-  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
-  const uint32_t lo0 = M0 * c[0], hi0 = __umulhi(M0, c[0]);
-  const uint32_t lo1 = M1 * c[2], hi1 = __umulhi(M1, c[2]);
-  const uint32_t n0 = hi1 ^ c[1] ^ k0, n1 = lo1, n2 = hi0 ^ c[3] ^ k1, n3 = lo0;
-  c[0] = n0;
-  c[1] = n1;
-  c[2] = n2;
-  c[3] = n3;
-}
-
-__device__ void philox4x32_10(uint32_t* c, uint32_t k0, uint32_t k1) {
-  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    philox_round(c, k0, k1);
-    k0 += W0;
-    k1 += W1;
-  }
-}
-
-__device__ __forceinline__ double u01_from(uint32_t a, uint32_t b) {
-  // 53 random bits -> [0, 1)
-  const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
-  return (double)m * (1.0 / 9007199254740992.0);
 }
 
 template <typename C>

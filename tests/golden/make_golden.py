@@ -9,9 +9,15 @@ stored beside the outputs, so the tests never need the reference.
 
 Usage:  python tests/golden/make_golden.py [--reference PATH] [--big]
         python tests/golden/make_golden.py --optimizer [--reference PATH]
+        python tests/golden/make_golden.py --projectors [--reference PATH]
 
 ``--big`` adds the McClean ZZ-chain cases at n = 18, 20 (L = 50), which take
 about two minutes of reference time.
+
+``--projectors`` writes ``projectors.npz``: the +1-projector probabilities
+||Pi_+ psi||^2 of every observable term (the reference's ``Projector``,
+``observable.py:126-177``, as ``sample_expec_val`` uses them,
+``base.py:22-33``) on the golden final states of the Pauli-sum cases.
 
 ``--optimizer`` writes ``optimizer.npz`` instead: the reference's own
 optimiser classes (``qradient/optimization.py``) fed seeded gradient and cost
@@ -263,12 +269,45 @@ def optimizer_main(reference):
     print("wrote", len(out), "arrays to optimizer.npz")
 
 
+def projectors_main(reference):
+    """Projector probabilities from the reference's Projector class.  The
+    snapshot's Observable.load_projectors calls a method that does not exist
+    (observable.py:85 calls check_observable; the method is the name-mangled
+    __check_observable of :106), so the projectors are built here in the
+    order load_projectors would build them (observable.py:88-103)."""
+    spec = importlib.util.spec_from_file_location(
+        "ref_observable", os.path.join(reference, "qradient", "physical_components", "observable.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    Projector = mod.Projector
+    gold = np.load(os.path.join(HERE, "golden.npz"))
+    out = {}
+    names = sorted({k.split("/")[1] for k in gold.files if k.startswith("mcclean/") and k.endswith("/state")})
+    for name in names:
+        key = "mcclean/" + name + "/"
+        kind, q0, q1, vec = gold[key + "kind"], gold[key + "q0"], gold[key + "q1"], gold[key + "state"]
+        n = int(np.log2(vec.size))
+        Projector.set_qnum(n)
+        probs = []
+        for k, a, b in zip(kind, q0, q1):
+            key_id = "xyz"[k] if k < 3 else "zz"
+            proj = Projector(key_id, int(a)) if k < 3 else Projector("zz", int(a), int(b))
+            probs.append((np.abs(proj.dot(vec)) ** 2).sum())
+        out[name + "/p_plus"] = np.array(probs)
+        print("projectors %-22s %d terms" % (name, len(probs)), flush=True)
+    np.savez_compressed(os.path.join(HERE, "projectors.npz"), **out)
+    print("wrote", len(out), "arrays to projectors.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--big", action="store_true")
     ap.add_argument("--optimizer", action="store_true")
+    ap.add_argument("--projectors", action="store_true")
     args = ap.parse_args()
+    if args.projectors:
+        return projectors_main(args.reference)
     if args.optimizer:
         return optimizer_main(args.reference)
     McClean, Qaoa = load_reference(args.reference)
