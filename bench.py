@@ -1,6 +1,6 @@
 """Benchmark of the McClean adjoint grad_run on GB300.
 
-Workload (the spec configuration): McClean n=24 qubits, L=50 layers,
+Workload: McClean n=24 qubits, L=50 layers,
 complex128, ZZ-chain observable sum_i Z_i Z_{i+1}, seeded random axes and
 angles (numpy default_rng(24)), the reference's CNOT-ladder-before-rotations
 layer.  A step is one full grad_run (E and all L*n gradients).
@@ -371,7 +371,7 @@ def serving_mix(seed, count):
 
 
 def run_serving(args):
-    """Poisson stream of the config-5 mix through the continuous-batching
+    """Poisson stream of a mixed McClean / QAOA request population through the continuous-batching
     server; compared with the plain per-call GPU path on the same requests."""
     import torch
 
@@ -418,7 +418,7 @@ def run_serving(args):
     line = {"metric": "served circuits/s (run + grad_run mix)", "value": value * world, "unit": "circuits/s",
             "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed f64/f32", "data": "synthetic Poisson stream",
-            "config": {"workload": "config-5 mix: 60%% McClean n~U{8..26} L~U{5..60}, 40%% QAOA 3-regular "
+            "config": {"workload": "mixed request stream: 60%% McClean n~U{8..26} L~U{5..60}, 40%% QAOA 3-regular "
                                    "n~U{10..24} p~U{1..6}, 70%% grad_run / 30%% run, dtype per request; "
                                    "%d requests, Poisson rate %.1f/s" % (len(reqs), rate)},
             "latency": st, "plain_per_call_circuits_s": plain, "speedup_vs_plain": value / plain,

@@ -85,8 +85,8 @@ def mcclean_cases(big):
         obs = {"zz": zz_pairs(n, [(0, 1)])} if n >= 2 else {"z": np.array([1.0], dtype=object)}
         cases.append(("zz01_n%d_L%d" % (n, L), n, L, 100 + 7 * n + L, obs, "cnot", False))
     # the CPU configuration of the benchmark: n=10, L=10, Z0 Z1, seed 0
-    cases.append(("config1_n10_L10", 10, 10, 0, {"zz": zz_pairs(10, [(0, 1)])}, "cnot", False))
-    cases.append(("config1_cz_n10_L10", 10, 10, 0, {"zz": zz_pairs(10, [(0, 1)])}, "cz", False))
+    cases.append(("zz01_seed0_n10_L10", 10, 10, 0, {"zz": zz_pairs(10, [(0, 1)])}, "cnot", False))
+    cases.append(("zz01_cz_seed0_n10_L10", 10, 10, 0, {"zz": zz_pairs(10, [(0, 1)])}, "cz", False))
     cases.append(("cz_n6_L4", 6, 4, 11, {"zz": zz_pairs(6, [(0, 1), (2, 5)])}, "cz", False))
     # general Pauli-sum observables
     for n, L, seed in [(5, 4, 21), (7, 3, 22), (9, 2, 23)]:

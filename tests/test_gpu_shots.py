@@ -23,7 +23,7 @@ from oracle import shots as OS
 
 pytestmark = pytest.mark.gpu
 
-SHIFT_CASES = ["pauli_n5_L4", "pauli_n7_L3", "config1_n10_L10", "cz_n6_L4", "ini_n6_L3", "zz01_n4_L3"]
+SHIFT_CASES = ["pauli_n5_L4", "pauli_n7_L3", "zz01_seed0_n10_L10", "cz_n6_L4", "ini_n6_L3", "zz01_n4_L3"]
 
 
 def _circuit(golden, name, dtype="complex128", components=False):
