@@ -128,6 +128,21 @@ int qg_sample_workspace_size(int n, size_t* bytes);
 int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t seed, uint64_t offset,
               void* workspace_dev, size_t workspace_bytes, int64_t* out_dev, qg_stream stream);
 
+/* ---- Tuning (no reference counterpart).  A sweep stages 2^tile_bits
+ * amplitudes in shared memory and applies every rotation on those bits in
+ * one pass (the fusion depth); ctas_per_sm sets the persistent grid (block
+ * shape across the SMs, capped at what fits).  0 restores the default
+ * (tile_bits 11 for complex128, 12 for complex64; ctas_per_sm from the
+ * occupancy query).  tile_bits: 5..12 for complex128, 6..13 for
+ * complex64 (the backward sweep holds two tiles in shared memory); tiles
+ * larger than the state use the whole state.  Call before launches that use the handle, not while
+ * another thread uses it; the workspace size may change with the setting.
+ * qg_get_tuning reports the effective values (tile bits after clamping to
+ * n, CTAs per SM of the backward sweeps).  The autotuner of
+ * qradient_gb300/tuning.py picks them by timing. */
+int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm);
+int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_sm);
+
 /* ---- Finite-shot estimates (the projector estimator of
  * ParametrizedCircuit.sample_expec_val / sample_component_expec_val,
  * base.py:22-46, with the projectors of observable.py:82-177).

@@ -39,6 +39,8 @@ SIGNATURES = {
     "qg_batch_workspace_size": (_I, [ctypes.POINTER(_SZ)]),
     "qg_batch_launch": (_I, [_I, _P, _I, _I, _I, _P, _SZ, _P]),
     "qg_grad_noalloc": (_I, [_P, _I, _P, _P, _P, _P, _P]),
+    "qg_set_tuning": (_I, [_P, _I, _I, _I]),
+    "qg_get_tuning": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "qg_pauli_workspace_size": (_I, [_P, ctypes.POINTER(_SZ)]),
     "qg_pauli_expectations": (_I, [_P, _I, _P, _P, _SZ, _P, _P]),
     "qg_projector_shots": (_I, [_I, _I, _P, _P, _I, ctypes.c_uint64, ctypes.c_uint64, _P, _P, _P]),

@@ -48,11 +48,15 @@ def _dev_bytes(arr, device):
 class Batch:
     """A fixed list of jobs executed together; parameters live in ``params``."""
 
-    def __init__(self, device=None, dtype="complex64", grad=True, use_graph=True):
+    def __init__(self, device=None, dtype="complex64", grad=True, use_graph=True, cluster_from=None):
+        """cluster_from: smallest qubit count whose jobs are split over a
+        2-CTA cluster (default: only jobs too large for one CTA);
+        ``tuning.tune_batch`` picks it by timing."""
         self.device = _native.require_cuda(device)
         self.dtype = _native.dtype_code(dtype)
         self.want_grad = grad
         self.use_graph = use_graph
+        self.cluster_from = SINGLE_MAX[self.dtype] + 1 if cluster_from is None else int(cluster_from)
         self._specs = []
         self._keep = []
         self._graph = None
@@ -95,10 +99,26 @@ class Batch:
             if s["init"] is not None:
                 self.params[-1].copy_(torch.as_tensor(np.asarray(s["init"], dtype=np.float64)).reshape(-1))
             off += s["nparams"]
+        self._structures = {}
+        self._build_groups()
+        self.finalized = True
+
+    def refinalize(self, cluster_from):
+        """Regroup the jobs with a new cluster split; parameters are kept."""
+        if not self.finalized:
+            self.cluster_from = int(cluster_from)
+            return self.finalize()
+        self.cluster_from = int(cluster_from)
+        self._graph = None
+        self._build_groups()
+
+    def _build_groups(self):
+        dev = self.device
         # shared structure buffers, one per distinct circuit object
-        cache = {}
+        cache = self._structures
         small, clus, big = [], [], []
         single, cmax = SINGLE_MAX[self.dtype], CLUSTER_MAX[self.dtype]
+        split = max(4, min(self.cluster_from, single + 1))
         for i, s in enumerate(self._specs):
             c = s["circuit"]
             key = id(c)
@@ -124,7 +144,7 @@ class Batch:
             job["cost_maxabs"] = st["cost_maxabs"]
             job["cost_w0"] = st["cost_w0"]
             job["cost"] = st["cost"].data_ptr() if st["cost"] is not None else 0
-            (small if c.qnum <= single else clus).append((c.qnum, job))
+            (small if c.qnum < split else clus).append((c.qnum, job))
         self._keep = list(cache.values())
         self._groups = []
         for cl, jobs in ((1, small), (2, clus)):
@@ -135,7 +155,6 @@ class Batch:
             ws = torch.zeros(256, dtype=torch.uint8, device=dev)
             self._groups.append((cl, _dev_bytes(arr, dev), len(jobs), maxq, ws))
         self._big = big
-        self.finalized = True
 
     def _structure(self, c, kind):
         dev = self.device

@@ -12,6 +12,8 @@ class ParametrizedCircuit:
     dtype      'complex128' (default, as the reference) or 'complex64'
     device     CUDA device (default: current)
     grad_mode  'auto' (default), 'history' or 'uncompute'
+    autotune   False (default) or True: time the kernel variants for this
+               circuit shape on first use (qradient_gb300.tuning)
     """
 
     def init(self, qubit_number, observable, use_observable_components=False, **kwargs):
@@ -28,6 +30,32 @@ class ParametrizedCircuit:
         self._native = None
         self._native_key = None
         self._weight_cache = {}
+        self.autotune = bool(kwargs.get("autotune", False))
+        self._tuning = {}  # dtype code -> (tile_bits, ctas_per_sm)
+
+    def _apply_tuning(self, nat):
+        for dt, v in self._tuning.items():
+            if not isinstance(dt, int):
+                continue
+            t, c = v
+            _lib.check(_lib.load().qg_set_tuning(nat._h, dt, int(t), int(c)))
+        return nat
+
+    def set_tuning(self, tile_bits=0, ctas_per_sm=0, dtype=None):
+        """Fix the sweep path's fusion depth and CTAs per SM (0: default)."""
+        dt = self._dtype_code if dtype is None else _native.dtype_code(dtype)
+        self._tuning[dt] = (int(tile_bits), int(ctas_per_sm))
+        if self._native is not None:
+            self._apply_tuning(self._native)
+
+    def _maybe_tune(self, op):
+        if self.autotune and ("tuned", self._dtype_code, op) not in self._tuning:
+            from .. import tuning
+
+            r = tuning.tune_circuit(self, op=op)
+            self._tuning[self._dtype_code] = (r["tile_bits"], r["ctas_per_sm"])
+            self._tuning[("tuned", self._dtype_code, op)] = r
+            self._apply_tuning(self.native())
 
     def _device(self):
         return _native.require_cuda(self.device)

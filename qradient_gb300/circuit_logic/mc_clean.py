@@ -59,8 +59,8 @@ class McClean(ParametrizedCircuit):
             raise ValueError("Invalid axis {}".format(bad.flat[0]))
         key = axes.astype(np.int32).tobytes()
         if self._native is None or self._native_key != key:
-            self._native = _native.NativeCircuit.mcclean(self.qnum, axes, self.observable.terms,
-                                                         _ENT[self.entangler], _PLACE[self.placement])
+            self._native = self._apply_tuning(_native.NativeCircuit.mcclean(
+                self.qnum, axes, self.observable.terms, _ENT[self.entangler], _PLACE[self.placement]))
             self._native_key = key
         return self._native
 
@@ -82,6 +82,7 @@ class McClean(ParametrizedCircuit):
     def run_expec_val(self, hide_progbar=True, exact_expec_val=True, shot_num=1, ini_state=None):
         """Run the circuit and return <psi|O|psi> (mc_clean.py:27-45), or its
         projector-shot estimate when exact_expec_val is False."""
+        self._maybe_tune("run")
         nat = self.native()
         dev = self._device()
         e, st = nat.run(self._angles(), self._dtype_code, dev, ini_state=ini_state, want_state=True)
@@ -92,6 +93,7 @@ class McClean(ParametrizedCircuit):
 
     def grad_run(self, hide_progbar=True, ini_state=None):
         """Expectation value and the full adjoint gradient [L, n] (mc_clean.py:47-78)."""
+        self._maybe_tune("grad")
         nat = self.native()
         dev = self._device()
         op = self._grad_op(nat)
@@ -100,6 +102,7 @@ class McClean(ParametrizedCircuit):
 
     def grad_run_tensors(self, angles=None, ini_state=None, out=None):
         """Device-side grad_run: (E tensor[1], grad tensor[L*n]) without host copies."""
+        self._maybe_tune("grad")
         nat = self.native()
         dev = self._device()
         op = self._grad_op(nat)

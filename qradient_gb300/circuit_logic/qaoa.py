@@ -32,6 +32,7 @@ class _Gates:
     def grad_run_tensors(self, params, ini_state=None, out=None):
         """Device-side grad_run: params [p, 2] (beta, gamma) as a tensor or
         array; returns (E tensor[1], grad tensor[2p]) without host copies."""
+        self._maybe_tune("grad")
         nat = self.native()
         return nat.grad(params, self._dtype_code, self._device(), self._grad_op(nat), ini_state=ini_state, out=out)
 
@@ -55,7 +56,8 @@ class Qaoa(ParametrizedCircuit):
 
     def native(self):
         if self._native is None:
-            self._native = _native.NativeCircuit.qaoa(self.qnum, self.lnum, self.observable.terms)
+            self._native = self._apply_tuning(_native.NativeCircuit.qaoa(self.qnum, self.lnum,
+                                                                         self.observable.terms))
         return self._native
 
     def __check_parameters(self, betas, gammas):
@@ -68,6 +70,7 @@ class Qaoa(ParametrizedCircuit):
 
     def run_expec_val(self, betas, gammas, hide_progbar=True, exact_expec_val=True, shot_num=1, ini_state=None):
         """Forward run and <psi|O|psi> (qaoa.py:23-38)."""
+        self._maybe_tune("run")
         params = self.__check_parameters(betas, gammas)
         nat = self.native()
         e, st = nat.run(params, self._dtype_code, self._device(), ini_state=ini_state, want_state=True)
@@ -78,6 +81,7 @@ class Qaoa(ParametrizedCircuit):
 
     def grad_run(self, betas, gammas, hide_progbar=True, ini_state=None):
         """E and grad [p, 2] (column 0: beta, column 1: gamma) (qaoa.py:40-70)."""
+        self._maybe_tune("grad")
         params = self.__check_parameters(betas, gammas)
         nat = self.native()
         op = self._grad_op(nat)
@@ -93,6 +97,7 @@ class Qaoa(ParametrizedCircuit):
     def grad_run_tensors(self, params, ini_state=None, out=None):
         """Device-side grad_run: params [p, 2] (beta, gamma) as a tensor or
         array; returns (E tensor[1], grad tensor[2p]) without host copies."""
+        self._maybe_tune("grad")
         nat = self.native()
         return nat.grad(params, self._dtype_code, self._device(), self._grad_op(nat), ini_state=ini_state, out=out)
 

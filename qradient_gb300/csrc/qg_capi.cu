@@ -68,6 +68,10 @@ struct qg_circuit {
   int cost_kind = COST_NONE;
   double cost_w0 = 1.0;
   int cost_maxabs = 0;
+  // tuning per dtype (0 = default): tile bits of a sweep (how many qubits
+  // one shared-memory pass fuses) and resident CTAs per SM
+  int tune_tile_bits[2] = {0, 0};
+  int tune_ctas[2] = {0, 0};
   IntTermList* iterms = nullptr;
   RealTermList* rterms = nullptr;
   ~qg_circuit() {
@@ -91,11 +95,19 @@ struct Layout {
 
 // Tile plan of one layer: A = bits [0, t); then sweeps over the remaining
 // high bits, each padded with the lowest bits (coalesced 128-byte runs).
-Layout make_layout(int n, int dtype) {
+// Largest tile whose backward sweep (two tiles plus the phase table) fits
+// the 227 KB of shared memory a CTA may use.
+int max_tile_bits(int dtype) { return dtype == QG_C128 ? TMAX - 1 : TMAX; }
+
+int default_tile_bits(int dtype) {
+  return dtype == QG_C128 ? env_int("QG_TILE_BITS_C128", 11) : env_int("QG_TILE_BITS_C64", 12);
+}
+
+Layout make_layout(int n, int dtype, int tile_bits) {
   Layout lay;
-  int t = dtype == QG_C128 ? env_int("QG_TILE_BITS_C128", 11) : env_int("QG_TILE_BITS_C64", 12);
-  t = std::max(4, std::min(t, TMAX));
+  int t = tile_bits > 0 ? tile_bits : default_tile_bits(dtype);
   const int c = dtype == QG_C128 ? 3 : 4;
+  t = std::max(c + 2, std::min(t, max_tile_bits(dtype)));
   if (n <= t) {
     lay.t = n;
     std::vector<int> all;
@@ -229,7 +241,7 @@ struct Program {
 
 int build_program(const qg_circuit* c, int dtype, bool with_ini, Program& P) {
   const int n = c->n;
-  P.lay = make_layout(n, dtype);
+  P.lay = make_layout(n, dtype, c->tune_tile_bits[dtype == QG_C64 ? 1 : 0]);
   P.sweeps.clear();
   if (c->kind == 0) {
     P.nparams = c->L * n;
@@ -381,7 +393,14 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
   const bool unc = op == QG_OP_GRAD_UNCOMPUTE;
   int per_bwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, true, unc) : sweep_ctas_per_sm<float>(big, true, unc);
   int per_fwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, false, false) : sweep_ctas_per_sm<float>(big, false, false);
-  per_bwd = env_int("QG_CTAS_PER_SM", per_bwd);
+  const int tuned = c->tune_ctas[dtype == QG_C64 ? 1 : 0];
+  if (tuned > 0) {
+    // never above what fits: the kernels assume every CTA of the grid is resident
+    per_bwd = std::min(per_bwd, tuned);
+    per_fwd = std::min(per_fwd, tuned);
+  } else {
+    per_bwd = env_int("QG_CTAS_PER_SM", per_bwd);
+  }
   w.G = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_bwd);
   w.grid_fwd = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_fwd);
   w.neslots = obs_sweeps_needed(c, P.lay, op != QG_OP_RUN);
@@ -920,6 +939,31 @@ int qg_sample(int n, int dtype, const void* state, int64_t nshots, uint64_t seed
     QG_CUDA(launch_sample<float2>(n, (const float2*)state, nshots, seed, offset, (double*)ws, out, st));
   else
     return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+  return QG_OK;
+}
+
+int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm) {
+  if (int s = check_circuit(c)) return s;
+  if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+  const int tmin = dtype == QG_C128 ? 5 : 6;
+  if (tile_bits != 0 && (tile_bits < tmin || tile_bits > max_tile_bits(dtype)))
+    return fail(QG_ERR_INVALID, "tile_bits %d outside %d..%d (0: default)", tile_bits, tmin, max_tile_bits(dtype));
+  if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(QG_ERR_INVALID, "ctas_per_sm %d outside 0..64", ctas_per_sm);
+  c->tune_tile_bits[dtype] = tile_bits;
+  c->tune_ctas[dtype] = ctas_per_sm;
+  return QG_OK;
+}
+
+int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_sm) {
+  if (int s = check_circuit(c)) return s;
+  if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
+  if (!tile_bits || !ctas_per_sm) return fail(QG_ERR_INVALID, "null output");
+  Program P;
+  if (int s = build_program(c, dtype, false, P)) return s;
+  WsLayout W = ws_layout(c, dtype, QG_OP_GRAD_HISTORY, P);
+  *tile_bits = P.lay.t;
+  const int sms = sm_count();
+  *ctas_per_sm = sms > 0 ? (W.G + sms - 1) / sms : W.G;
   return QG_OK;
 }
 

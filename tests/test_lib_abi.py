@@ -130,3 +130,36 @@ def test_optimiser_steps_and_component_gradient_validate_arguments():
         assert lib.qg_grad_component(h, 0, 1, fake, None, k, fake, 1 << 20, fake, fake, None) == INV
         assert b"component" in lib.qg_last_error()
     lib.qg_destroy(h)
+
+
+def test_tuning_knobs_validate_and_report():
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    st, h = _create(20, 2, np.zeros((2, 20)))
+    assert st == 0
+    INV = _lib.QG_ERR_INVALID
+    assert lib.qg_set_tuning(h, 0, 4, 0) == INV
+    assert lib.qg_set_tuning(h, 0, 13, 0) == INV
+    assert lib.qg_set_tuning(h, 1, 5, 0) == INV
+    assert lib.qg_set_tuning(h, 1, 13, 0) == 0
+    assert lib.qg_set_tuning(h, 5, 11, 0) == INV
+    assert lib.qg_set_tuning(h, 0, 11, -1) == INV
+    t, c = ctypes.c_int(), ctypes.c_int()
+    for bits in (10, 12, 0):
+        assert lib.qg_set_tuning(h, 0, bits, 0) == 0
+        assert lib.qg_get_tuning(h, 0, ctypes.byref(t), ctypes.byref(c)) == 0
+        assert t.value == (bits or 11)
+    # history workspace holds one state per sweep: deeper fusion, fewer sweeps
+    sizes = []
+    for bits in (10, 12):
+        lib.qg_set_tuning(h, 0, bits, 0)
+        b = ctypes.c_size_t()
+        lib.qg_workspace_size(h, 0, 1, ctypes.byref(b))
+        sizes.append(b.value)
+    assert sizes[0] > sizes[1]
+    lib.qg_destroy(h)
+    st, h = _create(6, 1, np.zeros((1, 6)))
+    assert lib.qg_set_tuning(h, 1, 12, 0) == 0
+    assert lib.qg_get_tuning(h, 1, ctypes.byref(t), ctypes.byref(c)) == 0 and t.value == 6
+    lib.qg_destroy(h)
