@@ -56,6 +56,8 @@ def parse():
                     help="mcclean: one n=24 L=50 circuit (headline); batched: 4096 parameter vectors of an "
                          "n=14 L=30 circuit in one graph replay; qaoa: 3-regular MaxCut grad_run")
     ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the sweep-path variants for this circuit first (untimed) and use the fastest")
     ap.add_argument("--p", type=int, default=10, help="QAOA depth")
     ap.add_argument("--requests", type=int, default=120, help="serving: requests in the Poisson stream")
     ap.add_argument("--rate", type=float, default=0.0, help="serving: arrivals per second (0: saturate)")
@@ -459,6 +461,12 @@ def main():
     out = (torch.empty(1, dtype=torch.float64, device=dev),
            torch.empty(args.n * args.layers, dtype=torch.float64, device=dev))
 
+    tuned = None
+    if args.autotune:
+        from qradient_gb300 import tuning
+
+        tuned = tuning.tune_circuit(circ, op="grad", use_cache=False)
+
     def step():
         circ.grad_run_tensors(angles_dev, out=out)
 
@@ -577,6 +585,15 @@ def main():
         "roofline": roof,
         "clocks": clk,
     }
+    from qradient_gb300 import tuning as _tuning
+
+    t_eff, c_eff = _tuning.get_tuning(circ.native(), circ._dtype_code)
+    line["config"]["tile_bits"] = t_eff
+    line["config"]["ctas_per_sm"] = c_eff
+    if tuned is not None:
+        line["config"]["autotune"] = {"chosen": [tuned["tile_bits"], tuned["ctas_per_sm"]],
+                                      "ms_by_candidate": {"%d/%d" % (r["tile_bits"], r["ctas_per_sm"]): r["ms"]
+                                                          for r in tuned["timings"]}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.n, args.layers, axes, angles, args.cpu_layers)
     if rank == 0:
