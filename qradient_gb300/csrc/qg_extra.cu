@@ -191,13 +191,18 @@ cudaError_t probe_fp64(double* scratch, size_t bytes, double* rate, cudaStream_t
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   const int threads = 256;
-  int blocks = sms * 8;
+  // exactly one wave of resident blocks: a partial second wave would leave
+  // SMs idle at the end and understate the rate
+  int per = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfma_probe_kernel, threads, 0);
+  if (e != cudaSuccess) return e;
+  int blocks = sms * (per > 0 ? per : 1);
   if ((size_t)blocks * threads * sizeof(double) > bytes) blocks = (int)(bytes / (threads * sizeof(double)));
   if (blocks < 1) return cudaErrorInvalidValue;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int iters = 1024;
+  const int iters = 4096;
   dfma_probe_kernel<<<blocks, threads, 0, st>>>(scratch, 64, 1.0000001, 1e-9);
   double best = 0.0;
   for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
