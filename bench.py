@@ -587,13 +587,14 @@ def main():
     }
     from qradient_gb300 import tuning as _tuning
 
-    t_eff, c_eff = _tuning.get_tuning(circ.native(), circ._dtype_code)
+    t_eff, c_eff, f_eff = _tuning.get_tuning(circ.native(), circ._dtype_code)
     line["config"]["tile_bits"] = t_eff
     line["config"]["ctas_per_sm"] = c_eff
+    line["config"]["forward_sweeps"] = "pipelined" if f_eff == _lib.QG_TUNE_FWD_PIPELINED else "plain"
     if tuned is not None:
-        line["config"]["autotune"] = {"chosen": [tuned["tile_bits"], tuned["ctas_per_sm"]],
-                                      "ms_by_candidate": {"%d/%d" % (r["tile_bits"], r["ctas_per_sm"]): r["ms"]
-                                                          for r in tuned["timings"]}}
+        line["config"]["autotune"] = {"chosen": [tuned["tile_bits"], tuned["ctas_per_sm"], tuned["flags"]],
+                                      "ms_by_candidate": {"%d/%d/%d" % (r["tile_bits"], r["ctas_per_sm"], r["flags"]):
+                                                          r["ms"] for r in tuned["timings"]}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.n, args.layers, axes, angles, args.cpu_layers)
     if rank == 0:

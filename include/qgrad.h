@@ -137,11 +137,17 @@ int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t 
  * complex64 (the backward sweep holds two tiles in shared memory); tiles
  * larger than the state use the whole state.  Call before launches that use the handle, not while
  * another thread uses it; the workspace size may change with the setting.
+ * flags: QG_TUNE_FWD_PIPELINED or QG_TUNE_FWD_PLAIN choose the forward
+ * sweep kernel (0: the default, pipelined).
  * qg_get_tuning reports the effective values (tile bits after clamping to
- * n, CTAs per SM of the backward sweeps).  The autotuner of
+ * n, CTAs per SM of the backward sweeps, the forward kernel flag).  The autotuner of
  * qradient_gb300/tuning.py picks them by timing. */
-int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm);
-int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_sm);
+enum {
+  QG_TUNE_FWD_PIPELINED = 1, /* forward sweeps prefetch the next tile (double-buffered) */
+  QG_TUNE_FWD_PLAIN = 2      /* forward sweeps load, compute, store (single buffer) */
+};
+int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm, int flags);
+int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_sm, int* flags);
 
 /* ---- Finite-shot estimates (the projector estimator of
  * ParametrizedCircuit.sample_expec_val / sample_component_expec_val,

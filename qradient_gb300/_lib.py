@@ -14,6 +14,7 @@ QG_ENT_NONE, QG_ENT_CNOT_LADDER, QG_ENT_CZ_LADDER = 0, 1, 2
 QG_PLACE_BEFORE, QG_PLACE_AFTER = 0, 1
 QG_PAULI_X, QG_PAULI_Y, QG_PAULI_Z, QG_PAULI_ZZ = 0, 1, 2, 3
 QG_OP_RUN, QG_OP_GRAD_HISTORY, QG_OP_GRAD_UNCOMPUTE = 0, 1, 2
+QG_TUNE_FWD_PIPELINED, QG_TUNE_FWD_PLAIN = 1, 2
 
 # every symbol include/qgrad.h declares, with its ctypes signature
 _P = ctypes.c_void_p
@@ -39,8 +40,8 @@ SIGNATURES = {
     "qg_batch_workspace_size": (_I, [ctypes.POINTER(_SZ)]),
     "qg_batch_launch": (_I, [_I, _P, _I, _I, _I, _P, _SZ, _P]),
     "qg_grad_noalloc": (_I, [_P, _I, _P, _P, _P, _P, _P]),
-    "qg_set_tuning": (_I, [_P, _I, _I, _I]),
-    "qg_get_tuning": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "qg_set_tuning": (_I, [_P, _I, _I, _I, _I]),
+    "qg_get_tuning": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "qg_pauli_workspace_size": (_I, [_P, ctypes.POINTER(_SZ)]),
     "qg_pauli_expectations": (_I, [_P, _I, _P, _P, _SZ, _P, _P]),
     "qg_projector_shots": (_I, [_I, _I, _P, _P, _I, ctypes.c_uint64, ctypes.c_uint64, _P, _P, _P]),

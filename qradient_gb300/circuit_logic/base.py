@@ -37,14 +37,15 @@ class ParametrizedCircuit:
         for dt, v in self._tuning.items():
             if not isinstance(dt, int):
                 continue
-            t, c = v
-            _lib.check(_lib.load().qg_set_tuning(nat._h, dt, int(t), int(c)))
+            t, c, f = v
+            _lib.check(_lib.load().qg_set_tuning(nat._h, dt, int(t), int(c), int(f)))
         return nat
 
-    def set_tuning(self, tile_bits=0, ctas_per_sm=0, dtype=None):
-        """Fix the sweep path's fusion depth and CTAs per SM (0: default)."""
+    def set_tuning(self, tile_bits=0, ctas_per_sm=0, flags=0, dtype=None):
+        """Fix the sweep path's fusion depth, CTAs per SM and forward kernel
+        (QG_TUNE_* flags); 0 keeps the default."""
         dt = self._dtype_code if dtype is None else _native.dtype_code(dtype)
-        self._tuning[dt] = (int(tile_bits), int(ctas_per_sm))
+        self._tuning[dt] = (int(tile_bits), int(ctas_per_sm), int(flags))
         if self._native is not None:
             self._apply_tuning(self._native)
 
@@ -53,7 +54,7 @@ class ParametrizedCircuit:
             from .. import tuning
 
             r = tuning.tune_circuit(self, op=op)
-            self._tuning[self._dtype_code] = (r["tile_bits"], r["ctas_per_sm"])
+            self._tuning[self._dtype_code] = (r["tile_bits"], r["ctas_per_sm"], r.get("flags", 0))
             self._tuning[("tuned", self._dtype_code, op)] = r
             self._apply_tuning(self.native())
 

@@ -72,6 +72,7 @@ struct qg_circuit {
   // one shared-memory pass fuses) and resident CTAs per SM
   int tune_tile_bits[2] = {0, 0};
   int tune_ctas[2] = {0, 0};
+  int tune_flags[2] = {0, 0};  // QG_TUNE_* bits
   IntTermList* iterms = nullptr;
   RealTermList* rterms = nullptr;
   ~qg_circuit() {
@@ -98,6 +99,16 @@ struct Layout {
 // Largest tile whose backward sweep (two tiles plus the phase table) fits
 // the 227 KB of shared memory a CTA may use.
 int max_tile_bits(int dtype) { return dtype == QG_C128 ? TMAX - 1 : TMAX; }
+
+// Forward sweeps that load their input use the double-buffered kernel?
+bool fwd_pipelined(const qg_circuit* c, int dtype) {
+  const int f = c->tune_flags[dtype == QG_C64 ? 1 : 0];
+  if (f & QG_TUNE_FWD_PIPELINED) return true;
+  if (f & QG_TUNE_FWD_PLAIN) return false;
+  // default on: measured 2.7% (complex128) and 5.5% (complex64) faster
+  // per McClean n=24 L=50 grad_run than the single-buffered forward sweeps
+  return env_int(dtype == QG_C128 ? "QG_FWD_PIPE_C128" : "QG_FWD_PIPE_C64", 1) != 0;
+}
 
 int default_tile_bits(int dtype) {
   return dtype == QG_C128 ? env_int("QG_TILE_BITS_C128", 11) : env_int("QG_TILE_BITS_C64", 12);
@@ -361,6 +372,7 @@ struct WsLayout {
   bool pingpong = false;  // a CNOT-ladder gather needs distinct in / out buffers
   int G = 1, grid_fwd = 1;
   int neslots = 1;
+  bool fwd_pipe = false;  // double-buffered forward sweeps
 };
 
 int obs_sweeps_needed(const qg_circuit* c, const Layout& lay, bool grad) {
@@ -392,7 +404,10 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
     if (d.nz > big.nz || (d.cost == COST_INT && big.cost != COST_INT)) big = d;
   const bool unc = op == QG_OP_GRAD_UNCOMPUTE;
   int per_bwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, true, unc) : sweep_ctas_per_sm<float>(big, true, unc);
-  int per_fwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, false, false) : sweep_ctas_per_sm<float>(big, false, false);
+  const bool pipe = fwd_pipelined(c, dtype);
+  w.fwd_pipe = pipe;
+  int per_fwd = dtype == QG_C128 ? sweep_ctas_per_sm<double>(big, false, false, pipe)
+                                 : sweep_ctas_per_sm<float>(big, false, false, pipe);
   const int tuned = c->tune_ctas[dtype == QG_C64 ? 1 : 0];
   if (tuned > 0) {
     // never above what fits: the kernels assume every CTA of the grid is resident
@@ -497,6 +512,9 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
         o.w = tm.w;
       }
       d->ndiag = k;
+      // weight runs (the terms are sorted by weight): the kernel sums the
+      // signs of a run in integers and multiplies by the weight once
+      for (int i = 0; i < k; ++i) d->term[i].endgrp = (int8_t)(i + 1 == k || d->term[i + 1].w != d->term[i].w);
     }
     int nxy = 0;
     for (const auto& tm : xy) {
@@ -549,7 +567,7 @@ int forward(const qg_circuit* c, const Program& P, const WsLayout& W, const doub
     p.psi_in = in;
     p.psi_out = out;
     ProfScope ps(0, st);
-    QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd, st));
+    QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd, st, W.fwd_pipe));
     in = out;
   }
   *final_state = in;
@@ -942,19 +960,23 @@ int qg_sample(int n, int dtype, const void* state, int64_t nshots, uint64_t seed
   return QG_OK;
 }
 
-int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm) {
+int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm, int flags) {
   if (int s = check_circuit(c)) return s;
   if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
   const int tmin = dtype == QG_C128 ? 5 : 6;
   if (tile_bits != 0 && (tile_bits < tmin || tile_bits > max_tile_bits(dtype)))
     return fail(QG_ERR_INVALID, "tile_bits %d outside %d..%d (0: default)", tile_bits, tmin, max_tile_bits(dtype));
   if (ctas_per_sm < 0 || ctas_per_sm > 64) return fail(QG_ERR_INVALID, "ctas_per_sm %d outside 0..64", ctas_per_sm);
+  if (flags & ~(QG_TUNE_FWD_PIPELINED | QG_TUNE_FWD_PLAIN) ||
+      (flags & QG_TUNE_FWD_PIPELINED && flags & QG_TUNE_FWD_PLAIN))
+    return fail(QG_ERR_INVALID, "bad tuning flags 0x%x", flags);
   c->tune_tile_bits[dtype] = tile_bits;
   c->tune_ctas[dtype] = ctas_per_sm;
+  c->tune_flags[dtype] = flags;
   return QG_OK;
 }
 
-int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_sm) {
+int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_sm, int* flags) {
   if (int s = check_circuit(c)) return s;
   if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
   if (!tile_bits || !ctas_per_sm) return fail(QG_ERR_INVALID, "null output");
@@ -964,6 +986,7 @@ int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_
   *tile_bits = P.lay.t;
   const int sms = sm_count();
   *ctas_per_sm = sms > 0 ? (W.G + sms - 1) / sms : W.G;
+  if (flags) *flags = W.fwd_pipe ? QG_TUNE_FWD_PIPELINED : QG_TUNE_FWD_PLAIN;
   return QG_OK;
 }
 

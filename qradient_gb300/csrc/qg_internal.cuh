@@ -110,7 +110,8 @@ struct ObsTerm {
   int8_t kind;    // 0 X, 1 Y, 2 Z, 3 ZZ
   int8_t b0, b1;  // global bit positions
   int8_t lb0;     // local tile bit of b0 (X/Y terms)
-  int32_t pad;
+  int8_t endgrp;  // diagonal terms: the last of a run of equal weights
+  int8_t pad[3];
   double w;
 };
 

@@ -9,12 +9,14 @@ namespace qg {
 // Record a failure message for qg_last_error() and return the status.
 int set_last_error(int status, const char* msg);
 
-// Resident CTAs per SM of a sweep kernel with this descriptor's shared memory.
+// Resident CTAs per SM of a sweep kernel with this descriptor's shared memory
+// (pipe: the double-buffered forward kernel).
 template <typename R>
-int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute);
+int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe = false);
 
+// pipe: use the double-buffered forward kernel for sweeps that load their input
 template <typename R>
-cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st);
+cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe = false);
 
 template <typename R>
 cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st);

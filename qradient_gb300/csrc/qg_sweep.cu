@@ -99,14 +99,6 @@ __device__ __forceinline__ C cneg(C a) {
   return a;
 }
 
-// (E psi)[x] for the entangler E: a gather for the CNOT ladder, a sign for CZ.
-template <typename C>
-__device__ __forceinline__ C load_pre(const C* psi, uint64_t x, int ent, const LadderMasks& lm) {
-  C v = psi[ent == ENT_CNOT ? ladder_inv(x, lm) : x];
-  if (ent == ENT_CZ && cz_negative(x)) v = cneg(v);
-  return v;
-}
-
 template <typename R>
 __device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
@@ -627,6 +619,101 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   }
 }
 
+// ------------------------------------------------------------ pipelined forward sweep
+//
+// The same sweep for an input loaded from memory, with the next tile's loads
+// in flight while the current tile is computed: each CTA owns two tile
+// buffers; the loads of tile i+1 are issued as asynchronous global->shared
+// copies (cp.async, one amplitude each, gathered through the CNOT ladder
+// where the sweep starts with it) before tile i's gates run.  The diagonal
+// and the CZ sign, which the plain kernel applies on load, run as a pass
+// over each thread's own landed elements.
+
+__device__ __forceinline__ void cp_async_elem(void* dst_smem, const double2* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_elem(void* dst_smem, const float2* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <typename R>
+__global__ void __launch_bounds__(NTHREADS) sweep_fwd_pipe_kernel(const __grid_constant__ SweepDesc d,
+                                                                  SweepPtrs<R> p) {
+  using C = typename C2T<R>::T;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ SetupShared S;
+  const int t = d.t, n = d.n;
+  const int tsize = 1 << t;
+  C* buf0 = (C*)smem;
+  C* ztab = buf0 + 2 * tsize;
+  C* ctab = ztab + (1 << d.nz);
+  sweep_setup<C, false>(d, p.params, S, ztab, ctab);
+
+  const int tid = threadIdx.x;
+  const LadderMasks lm = ladder_masks(n);
+  const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
+  const bool active = tid < tsize;
+  const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int64_t ntiles = (int64_t)1 << (n - t);
+  const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
+  const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
+
+  // copies of one tile into dst: this thread's elements only
+  auto issue = [&](int64_t tileid, C* dst) {
+    if (active) {
+      const int64_t base = deposit(tileid, S.outside, n - t);
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        const uint64_t src = d.pre == ENT_CNOT ? ladder_inv(x, lm) : x;
+        cp_async_elem(&dst[sw<R>(e)], p.psi_in + src);
+      }
+    }
+    cp_async_commit();
+  };
+
+  int cur = 0;
+  if ((int64_t)blockIdx.x < ntiles) issue(blockIdx.x, buf0);
+  for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
+    C* tile = buf0 + cur * tsize;
+    const int64_t nxt = tileid + gridDim.x;
+    if (nxt < ntiles)
+      issue(nxt, buf0 + (cur ^ 1) * tsize);
+    else
+      cp_async_commit();  // an empty group keeps the count of pending groups uniform
+    cp_async_wait<1>();   // this thread's copies of the current tile have landed
+    const int64_t base = deposit(tileid, S.outside, n - t);
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        C v = tile[sw<R>(e)];
+        if (d.pre == ENT_CZ && cz_negative(x)) v = cneg(v);
+        tile[sw<R>(e)] = apply_diag<C>(v, x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
+      }
+    }
+    __syncthreads();
+    apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
+    if (active) {
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        p.psi_out[x] = tile[sw<R>(e)];
+      }
+    }
+    __syncthreads();  // the buffer is refilled by the copies issued next iteration
+    cur ^= 1;
+  }
+  cp_async_wait<0>();
+}
+
 // ------------------------------------------------------------ backward sweep
 //
 // Loads lambda and psi at the point after the sweep's gates, accumulates
@@ -687,12 +774,23 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
     const int64_t base = deposit(tileid, S.outside, n - t);
     R tT = (R)0, tG = (R)0;
     if (active) {
+      // all of this thread's loads of the tile in flight at once (asynchronous
+      // global->shared copies), then one wait: a load-use loop would wait one
+      // memory round trip per element
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
         // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y]
-        C l = p.lam_in[d.lam_undo == ENT_CNOT ? ladder_fwd(x, lm) : x];
-        C q = p.psi_in[d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x];
+        cp_async_elem(&tl[sw<R>(e)], p.lam_in + (d.lam_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
+        cp_async_elem(&tp[sw<R>(e)], p.psi_in + (d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
+      }
+      cp_async_commit();
+      cp_async_wait<0>();
+      for (int k = 0; k < nk; ++k) {
+        const int e = tid + k * NTHREADS;
+        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+        C l = tl[sw<R>(e)];
+        C q = tp[sw<R>(e)];
         if (d.lam_undo == ENT_CZ && cz_negative(x)) l = cneg(l);
         if (d.psi_undo == ENT_CZ && cz_negative(x)) q = cneg(q);
         if (need_w) {
@@ -834,19 +932,26 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
   double eacc = 0.0;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, outside, n - t);
-    if (d.nxy > 0) {
-      if (active)
+    if (active) {
+      // every load of this thread's elements in flight at once, then one wait
+      for (int k = 0; k < nk; ++k) {
+        const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
+        cp_async_elem(&tile[sw<R>(tid + k * NTHREADS)], psi + (d.pre == ENT_CNOT ? ladder_inv(x, lm) : x));
+      }
+      cp_async_commit();
+      cp_async_wait<0>();
+      if (d.pre == ENT_CZ)
         for (int k = 0; k < nk; ++k) {
           const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
-          tile[sw<R>(tid + k * NTHREADS)] = load_pre<C>(psi, x, d.pre, lm);
+          if (cz_negative(x)) tile[sw<R>(tid + k * NTHREADS)] = cneg(tile[sw<R>(tid + k * NTHREADS)]);
         }
-      __syncthreads();
     }
+    if (d.nxy > 0) __syncthreads();  // X/Y terms read partners other threads loaded
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
-        const C v = d.nxy > 0 ? tile[sw<R>(e)] : load_pre<C>(psi, x, d.pre, lm);
+        const C v = tile[sw<R>(e)];
         double lx = 0.0, ly = 0.0;
         if (d.cost == COST_INT || d.cost == COST_REAL || d.ndiag > 0) {
           double dv = 0.0;
@@ -855,20 +960,17 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
           } else if (d.cost == COST_REAL) {
             dv = cost_d[x];
           } else {
+            // integer sign sums per run of equal weights, one multiply per run
             int cnt = 0;
-            double wcur = d.term[0].w;
             for (int i = 0; i < d.ndiag; ++i) {
               const ObsTerm& tm = d.term[i];
-              if (tm.w != wcur) {
-                dv = fma(wcur, (double)cnt, dv);
+              const uint64_t m = (1ull << tm.b0) | (tm.kind == 3 ? (1ull << tm.b1) : 0ull);
+              cnt += 1 - 2 * (__popcll(x & m) & 1);
+              if (tm.endgrp) {
+                dv = fma(tm.w, (double)cnt, dv);
                 cnt = 0;
-                wcur = tm.w;
               }
-              int s = (int)((x >> tm.b0) & 1);
-              if (tm.kind == 3) s ^= (int)((x >> tm.b1) & 1);
-              cnt += 1 - 2 * s;
             }
-            dv = fma(wcur, (double)cnt, dv);
           }
           lx = dv * (double)v.x;
           ly = dv * (double)v.y;
@@ -987,20 +1089,23 @@ __global__ void finalize_kernel(const double* partials, int G, int kind, int n, 
 // ------------------------------------------------------------ launchers
 
 template <typename R>
-static size_t sweep_smem(const SweepDesc& d, bool bwd) {
+static size_t sweep_smem(const SweepDesc& d, bool bwd, bool pipe = false) {
   using C = typename C2T<R>::T;
-  size_t s = (size_t)(bwd ? 2 : 1) * ((size_t)1 << d.t) * sizeof(C);
+  size_t s = (size_t)(bwd || pipe ? 2 : 1) * ((size_t)1 << d.t) * sizeof(C);
   s += ((size_t)1 << d.nz) * sizeof(C);
   if (d.cost == COST_INT) s += (size_t)(2 * d.cost_maxabs + 1) * sizeof(C);
   return s;
 }
 
 template <typename R>
-int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute) {
-  const size_t smem = sweep_smem<R>(d, bwd);
+int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe) {
+  const size_t smem = sweep_smem<R>(d, bwd, pipe && !bwd);
   int blocks = 0;
   cudaError_t e;
-  if (!bwd) {
+  if (!bwd && pipe) {
+    cudaFuncSetAttribute(sweep_fwd_pipe_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_pipe_kernel<R>, NTHREADS, smem);
+  } else if (!bwd) {
     cudaFuncSetAttribute(sweep_fwd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_kernel<R>, NTHREADS, smem);
   } else if (uncompute) {
@@ -1017,11 +1122,19 @@ int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute) {
   return blocks > 0 ? blocks : 1;
 }
 
-template int sweep_ctas_per_sm<double>(const SweepDesc&, bool, bool);
-template int sweep_ctas_per_sm<float>(const SweepDesc&, bool, bool);
+template int sweep_ctas_per_sm<double>(const SweepDesc&, bool, bool, bool);
+template int sweep_ctas_per_sm<float>(const SweepDesc&, bool, bool, bool);
 
 template <typename R>
-cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st) {
+cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe) {
+  if (pipe && d.start == START_LOAD) {
+    const size_t smem = sweep_smem<R>(d, false, true);
+    cudaError_t e =
+        cudaFuncSetAttribute(sweep_fwd_pipe_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    sweep_fwd_pipe_kernel<R><<<grid, NTHREADS, smem, st>>>(d, p);
+    return cudaGetLastError();
+  }
   const size_t smem = sweep_smem<R>(d, false);
   cudaError_t e = cudaFuncSetAttribute(sweep_fwd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1050,7 +1163,7 @@ cudaError_t launch_observable(const ObsDesc& d, const typename C2T<R>::T* psi, t
                               const int32_t* cost_i, const double* cost_d, double* partials, int G, int grid,
                               cudaStream_t st) {
   using C = typename C2T<R>::T;
-  const size_t smem = d.nxy > 0 ? ((size_t)1 << d.t) * sizeof(C) : 0;
+  const size_t smem = ((size_t)1 << d.t) * sizeof(C);
   cudaError_t e = cudaFuncSetAttribute(observable_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   observable_kernel<R><<<grid, NTHREADS, smem, st>>>(d, psi, lam, cost_i, cost_d, partials, G);
@@ -1073,8 +1186,8 @@ cudaError_t launch_finalize(const double* partials, int G, int kind, int n, int 
   return cudaGetLastError();
 }
 
-template cudaError_t launch_sweep_fwd<double>(const SweepDesc&, const SweepPtrs<double>&, int, cudaStream_t);
-template cudaError_t launch_sweep_fwd<float>(const SweepDesc&, const SweepPtrs<float>&, int, cudaStream_t);
+template cudaError_t launch_sweep_fwd<double>(const SweepDesc&, const SweepPtrs<double>&, int, cudaStream_t, bool);
+template cudaError_t launch_sweep_fwd<float>(const SweepDesc&, const SweepPtrs<float>&, int, cudaStream_t, bool);
 template cudaError_t launch_sweep_bwd<double>(const SweepDesc&, const SweepPtrs<double>&, bool, int, cudaStream_t);
 template cudaError_t launch_sweep_bwd<float>(const SweepDesc&, const SweepPtrs<float>&, bool, int, cudaStream_t);
 template cudaError_t launch_observable<double>(const ObsDesc&, const double2*, double2*, const int32_t*, const double*,

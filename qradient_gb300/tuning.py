@@ -3,7 +3,9 @@
 Sweep path (one circuit per launch sequence): a sweep stages 2^t amplitudes
 in shared memory and applies every rotation on those t bits in one pass, so
 t is the fusion depth (fewer, larger passes against more shared memory per
-CTA and fewer resident CTAs); the persistent grid is CTAs-per-SM x SMs.
+CTA and fewer resident CTAs); the persistent grid is CTAs-per-SM x SMs; the
+forward sweeps either load, compute and store one tile at a time or keep
+the next tile's loads in flight in a second buffer.
 ``tune_circuit`` times grad_run (or run) for each candidate on a shortened
 copy of the circuit (same qubits, axes of the first layers) and applies the
 fastest to the circuit's handle (``qg_set_tuning``).
@@ -71,23 +73,25 @@ def _device_tag(device):
     return torch.cuda.get_device_name(device).replace(" ", "_")
 
 
-def set_tuning(native, dtype, tile_bits=0, ctas_per_sm=0):
-    _lib.check(_lib.load().qg_set_tuning(native._h, dtype, int(tile_bits), int(ctas_per_sm)))
+def set_tuning(native, dtype, tile_bits=0, ctas_per_sm=0, flags=0):
+    _lib.check(_lib.load().qg_set_tuning(native._h, dtype, int(tile_bits), int(ctas_per_sm), int(flags)))
 
 
 def get_tuning(native, dtype):
-    t, c = ctypes.c_int(0), ctypes.c_int(0)
-    _lib.check(_lib.load().qg_get_tuning(native._h, dtype, ctypes.byref(t), ctypes.byref(c)))
-    return t.value, c.value
+    """Effective (tile_bits, ctas_per_sm, flags) of a handle."""
+    t, c, f = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    _lib.check(_lib.load().qg_get_tuning(native._h, dtype, ctypes.byref(t), ctypes.byref(c), ctypes.byref(f)))
+    return t.value, c.value, f.value
 
 
 def sweep_candidates(dtype, n):
-    """(tile_bits, ctas_per_sm) pairs: three fusion depths around the
-    default, each at the occupancy-sized grid and at 1 CTA per SM."""
+    """(tile_bits, ctas_per_sm, flags) triples: three fusion depths around
+    the default, each at the occupancy-sized grid and at 1 CTA per SM, with
+    plain and with pipelined (double-buffered) forward sweeps."""
     depths = (10, 11, 12) if dtype == _lib.QG_C128 else (11, 12, 13)
     lo = 5 if dtype == _lib.QG_C128 else 6
     depths = sorted({max(lo, min(t, n)) for t in depths})
-    return [(t, c) for t in depths for c in (0, 1)]
+    return [(t, c, f) for t in depths for c in (0, 1) for f in (_lib.QG_TUNE_FWD_PLAIN, _lib.QG_TUNE_FWD_PIPELINED)]
 
 
 def _time_ms(fn, reps):
@@ -138,7 +142,7 @@ def tune_circuit(circuit, op="grad", reps=3, layers=4, candidates=None, use_cach
     if use_cache and candidates is None:
         hit = _load().get(key)
         if hit is not None:
-            set_tuning(circuit.native(), dtype, hit["tile_bits"], hit["ctas_per_sm"])
+            set_tuning(circuit.native(), dtype, hit["tile_bits"], hit["ctas_per_sm"], hit.get("flags", 0))
             return hit
     nat, nparams = _probe_circuit(circuit, layers)
     params = torch.rand(max(nparams, 1), dtype=torch.float64, device=dev)[:nparams] * 2 * np.pi
@@ -146,20 +150,20 @@ def tune_circuit(circuit, op="grad", reps=3, layers=4, candidates=None, use_cach
     g = torch.empty(max(nparams, 1), dtype=torch.float64, device=dev)
     gop = _native.choose_grad_op(nat, dtype, dev, getattr(circuit, "grad_mode", "auto"))
     timings = []
-    for t, c in candidates or sweep_candidates(dtype, circuit.qnum):
-        set_tuning(nat, dtype, t, c)
+    for t, c, f in candidates or sweep_candidates(dtype, circuit.qnum):
+        set_tuning(nat, dtype, t, c, f)
         if op == "grad":
             ws = nat.workspace(dtype, gop, dev)
             fn = lambda: nat.grad(params, dtype, dev, gop, workspace=ws, out=(e, g))  # noqa: E731
         else:
             ws = nat.workspace(dtype, _lib.QG_OP_RUN, dev)
             fn = lambda: nat.run_into(params, dtype, dev, None, ws, e, None)  # noqa: E731
-        timings.append({"tile_bits": t, "ctas_per_sm": c, "ms": _time_ms(fn, reps)})
+        timings.append({"tile_bits": t, "ctas_per_sm": c, "flags": f, "ms": _time_ms(fn, reps)})
         nat.release_workspaces()
     best = min(timings, key=lambda r: r["ms"])
-    result = {"tile_bits": best["tile_bits"], "ctas_per_sm": best["ctas_per_sm"], "ms": best["ms"],
-              "timings": timings}
-    set_tuning(circuit.native(), dtype, best["tile_bits"], best["ctas_per_sm"])
+    result = {"tile_bits": best["tile_bits"], "ctas_per_sm": best["ctas_per_sm"], "flags": best["flags"],
+              "ms": best["ms"], "timings": timings}
+    set_tuning(circuit.native(), dtype, best["tile_bits"], best["ctas_per_sm"], best["flags"])
     if use_cache and candidates is None:
         _store(key, result)
     return result

@@ -36,12 +36,12 @@ def test_every_candidate_matches_reference(golden, dtype, tol):
         circ, c = _golden_circuit(golden, name, dtype)
         for mode in ("history", "uncompute"):
             circ.grad_mode = mode
-            extra = [(9, 2), (6, 0)] + ([(13, 0)] if dtype == "complex64" else [(5, 0)])
-            for t, ctas in tuning.sweep_candidates(circ._dtype_code, circ.qnum) + extra:
-                circ.set_tuning(t, ctas)
+            extra = [(9, 2, 1), (6, 0, 1), (6, 0, 2)] + ([(13, 0, 1)] if dtype == "complex64" else [(5, 0, 1)])
+            for t, ctas, f in tuning.sweep_candidates(circ._dtype_code, circ.qnum) + extra:
+                circ.set_tuning(t, ctas, f)
                 E, g = circ.grad_run()
-                assert abs(E - float(c["e_grad"])) <= tol * max(1.0, abs(float(c["e_grad"]))), (name, t, ctas)
-                assert rel_err(g, c["grad"]) <= tol, (name, mode, t, ctas, rel_err(g, c["grad"]))
+                assert abs(E - float(c["e_grad"])) <= tol * max(1.0, abs(float(c["e_grad"]))), (name, t, ctas, f)
+                assert rel_err(g, c["grad"]) <= tol, (name, mode, t, ctas, f, rel_err(g, c["grad"]))
                 assert abs(circ.run_expec_val() - float(c["e_run"])) <= tol * max(1.0, abs(float(c["e_run"])))
 
 
@@ -52,10 +52,10 @@ def test_qaoa_candidates_match_reference(golden):
         c = golden.case("qaoa", name)
         n = int(max(c["q1"].max(), c["q0"].max())) + 1
         q = Qaoa(n, obs_dict(n, c["kind"], c["q0"], c["q1"], c["w"]), c["betas"].size)
-        for t, ctas in tuning.sweep_candidates(q._dtype_code, n):
-            q.set_tuning(t, ctas)
+        for t, ctas, f in tuning.sweep_candidates(q._dtype_code, n):
+            q.set_tuning(t, ctas, f)
             E, g = q.grad_run(c["betas"], c["gammas"])
-            assert rel_err(g, c["grad"]) <= 1e-12, (name, t, ctas)
+            assert rel_err(g, c["grad"]) <= 1e-12, (name, t, ctas, f)
 
 
 def test_tuner_picks_applies_and_caches(golden, tmp_path, monkeypatch):
@@ -64,11 +64,11 @@ def test_tuner_picks_applies_and_caches(golden, tmp_path, monkeypatch):
     monkeypatch.setenv("QG_TUNING_CACHE", str(tmp_path / "tune.json"))
     circ, c = _golden_circuit(golden, "chain_n16_L50", "complex128")
     r = tuning.tune_circuit(circ, op="grad", reps=2)
-    assert (r["tile_bits"], r["ctas_per_sm"]) in tuning.sweep_candidates(circ._dtype_code, 16)
+    assert (r["tile_bits"], r["ctas_per_sm"], r["flags"]) in tuning.sweep_candidates(circ._dtype_code, 16)
     assert len(r["timings"]) == len(tuning.sweep_candidates(circ._dtype_code, 16))
     assert all(t["ms"] > 0 for t in r["timings"])
-    t_eff, _ = tuning.get_tuning(circ.native(), circ._dtype_code)
-    assert t_eff == min(r["tile_bits"], 16)
+    t_eff, _, f_eff = tuning.get_tuning(circ.native(), circ._dtype_code)
+    assert t_eff == min(r["tile_bits"], 16) and f_eff == r["flags"]
     data = json.load(open(tmp_path / "tune.json"))
     assert len(data) == 1
     # a second circuit of the same shape takes the cached choice without timing

@@ -139,27 +139,30 @@ def test_tuning_knobs_validate_and_report():
     st, h = _create(20, 2, np.zeros((2, 20)))
     assert st == 0
     INV = _lib.QG_ERR_INVALID
-    assert lib.qg_set_tuning(h, 0, 4, 0) == INV
-    assert lib.qg_set_tuning(h, 0, 13, 0) == INV
-    assert lib.qg_set_tuning(h, 1, 5, 0) == INV
-    assert lib.qg_set_tuning(h, 1, 13, 0) == 0
-    assert lib.qg_set_tuning(h, 5, 11, 0) == INV
-    assert lib.qg_set_tuning(h, 0, 11, -1) == INV
-    t, c = ctypes.c_int(), ctypes.c_int()
-    for bits in (10, 12, 0):
-        assert lib.qg_set_tuning(h, 0, bits, 0) == 0
-        assert lib.qg_get_tuning(h, 0, ctypes.byref(t), ctypes.byref(c)) == 0
+    assert lib.qg_set_tuning(h, 0, 4, 0, 0) == INV
+    assert lib.qg_set_tuning(h, 0, 13, 0, 0) == INV
+    assert lib.qg_set_tuning(h, 1, 5, 0, 0) == INV
+    assert lib.qg_set_tuning(h, 1, 13, 0, 0) == 0
+    assert lib.qg_set_tuning(h, 5, 11, 0, 0) == INV
+    assert lib.qg_set_tuning(h, 0, 11, -1, 0) == INV
+    assert lib.qg_set_tuning(h, 0, 11, 0, 3) == INV
+    assert lib.qg_set_tuning(h, 0, 11, 0, 4) == INV
+    t, c, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    for bits, flags in ((10, 1), (12, 2), (0, 0)):
+        assert lib.qg_set_tuning(h, 0, bits, 0, flags) == 0
+        assert lib.qg_get_tuning(h, 0, ctypes.byref(t), ctypes.byref(c), ctypes.byref(f)) == 0
         assert t.value == (bits or 11)
+        assert f.value in (1, 2) and (flags == 0 or f.value == flags)
     # history workspace holds one state per sweep: deeper fusion, fewer sweeps
     sizes = []
     for bits in (10, 12):
-        lib.qg_set_tuning(h, 0, bits, 0)
+        lib.qg_set_tuning(h, 0, bits, 0, 0)
         b = ctypes.c_size_t()
         lib.qg_workspace_size(h, 0, 1, ctypes.byref(b))
         sizes.append(b.value)
     assert sizes[0] > sizes[1]
     lib.qg_destroy(h)
     st, h = _create(6, 1, np.zeros((1, 6)))
-    assert lib.qg_set_tuning(h, 1, 12, 0) == 0
-    assert lib.qg_get_tuning(h, 1, ctypes.byref(t), ctypes.byref(c)) == 0 and t.value == 6
+    assert lib.qg_set_tuning(h, 1, 12, 0, 0) == 0
+    assert lib.qg_get_tuning(h, 1, ctypes.byref(t), ctypes.byref(c), None) == 0 and t.value == 6
     lib.qg_destroy(h)
