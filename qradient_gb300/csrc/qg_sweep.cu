@@ -229,6 +229,17 @@ __device__ __forceinline__ void rot_block_any(C* el, int axis, int form, R u) {
 
 // ------------------------------------------------------------ shared setup
 
+// Index into the merged Z-rotation table: bit j = the amplitude's bit at the
+// j-th Z rotation.  An index x = base | dep_lo | offhi[k] combines disjoint
+// bit sets, so its pattern is the OR of the three parts' patterns (per tile,
+// per thread, per element-loop step).
+__device__ __forceinline__ int zpattern(uint64_t x, const SweepDesc& d) {
+  int pat = 0;
+  for (int j = 0; j < d.nz; ++j) pat |= (int)((x >> d.z[j].gbit) & 1) << j;
+  return pat;
+}
+
+
 // reduction slots of one CTA: X/Y rotations, U_j of the Z rotations, the
 // element total T, the gamma reduction
 constexpr int RS_XY = 0, RS_Z = TMAX, RS_T = TMAX + ZMAX, RS_G = TMAX + ZMAX + 1, RS_N = TMAX + ZMAX + 2;
@@ -243,6 +254,7 @@ struct SetupShared {
   int zk[ZMAX];        // Z rotation bit: k bit of the element loop (>= 0), thread bit (-1), outside (-2)
   int zkmask;          // k bits carrying a Z rotation
   int64_t offhi[32];   // deposit(k << 8) for the element loop
+  int zpk[32];         // Z-table index bits contributed by offhi[k]
   uint8_t outside[QMAX];
   double startP[QMAX + 1];
   double red[NTHREADS / 32][RS_N];
@@ -291,9 +303,13 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
   }
   for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;
   if (t > 8) {
-    for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
+    for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) {
+      S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
+      S.zpk[k] = zpattern((uint64_t)S.offhi[k], d);
+    }
   } else if (tid == 0) {
     S.offhi[0] = 0;
+    S.zpk[0] = 0;
   }
   if (tid == 0) {
     // bits not in the tile, ascending
@@ -359,16 +375,10 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
   __syncthreads();
 }
 
-__device__ __forceinline__ int zpattern(uint64_t x, const SweepDesc& d) {
-  int pat = 0;
-  for (int j = 0; j < d.nz; ++j) pat |= (int)((x >> d.z[j].gbit) & 1) << j;
-  return pat;
-}
-
 // Per-amplitude diagonal work of a sweep at index x: the cost phase and the
 // merged Z-rotation table (forward tables, or conjugated ones backward).
 template <typename C>
-__device__ __forceinline__ C apply_diag(C v, uint64_t x, const SweepDesc& d, const C* ztab, const C* ctab,
+__device__ __forceinline__ C apply_diag(C v, uint64_t x, int zpat, const SweepDesc& d, const C* ztab, const C* ctab,
                                         const int32_t* cost_i, const double* cost_d, double gamma, bool fold,
                                         bool bwd) {
   if (d.cost == COST_INT) {
@@ -380,7 +390,7 @@ __device__ __forceinline__ C apply_diag(C v, uint64_t x, const SweepDesc& d, con
   }
   if (d.has_diag && !fold) {
     if (d.nz)
-      v = cmul(v, ztab[zpattern(x, d)]);
+      v = cmul(v, ztab[zpat]);
     else
       v = cscale(v, ztab[0].x);
   }
@@ -580,6 +590,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int zpt = zpattern((uint64_t)dep_lo, d);
   const int64_t ntiles = (int64_t)1 << (n - t);
   const R plus = (R)exp2(-0.5 * n);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
@@ -587,6 +598,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
 
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
+    const int zp = zpt | zpattern((uint64_t)base, d);
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
@@ -603,7 +615,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
           v.y = (R)0;
         }
         if (d.pre == ENT_CZ && cz_negative(x)) v = cneg(v);
-        tile[sw<R>(e)] = apply_diag<C>(v, x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
+        tile[sw<R>(e)] = apply_diag<C>(v, x, zp | S.zpk[k], d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
       }
     }
     __syncthreads();
@@ -644,7 +656,7 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(NTHREADS) sweep_fwd_pipe_kernel(const __grid_constant__ SweepDesc d,
+__global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pipe_kernel(const __grid_constant__ SweepDesc d,
                                                                   SweepPtrs<R> p) {
   using C = typename C2T<R>::T;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -661,6 +673,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_pipe_kernel(const __grid_c
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int zpt = zpattern((uint64_t)dep_lo, d);
   const int64_t ntiles = (int64_t)1 << (n - t);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
@@ -690,13 +703,14 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_pipe_kernel(const __grid_c
       cp_async_commit();  // an empty group keeps the count of pending groups uniform
     cp_async_wait<1>();   // this thread's copies of the current tile have landed
     const int64_t base = deposit(tileid, S.outside, n - t);
+    const int zp = zpt | zpattern((uint64_t)base, d);
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
         C v = tile[sw<R>(e)];
         if (d.pre == ENT_CZ && cz_negative(x)) v = cneg(v);
-        tile[sw<R>(e)] = apply_diag<C>(v, x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
+        tile[sw<R>(e)] = apply_diag<C>(v, x, zp | S.zpk[k], d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
       }
     }
     __syncthreads();
@@ -727,8 +741,10 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_pipe_kernel(const __grid_c
 // bit j set).  U_j needs a per-element add only when bit j varies inside a
 // thread's element loop; otherwise the thread's tile total is added once.
 
+// At least 3 resident CTAs per SM for complex64 (its two tiles take 72 KB
+// of shared memory) and 2 for complex128: caps registers at 85 / 128.
 template <typename R, bool UNCOMPUTE>
-__global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_constant__ SweepDesc d, SweepPtrs<R> p) {
+__global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_kernel(const __grid_constant__ SweepDesc d, SweepPtrs<R> p) {
   using C = typename C2T<R>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SetupShared S;
@@ -745,10 +761,12 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
+  const int zpt = zpattern((uint64_t)dep_lo, d);
   const int64_t ntiles = (int64_t)1 << (n - t);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
   const bool need_w = d.nz > 0 || d.gslot >= 0;
+  const R w0r = (R)d.cost_w0;
   // Uncomputing psi: the scaled inverse rotations return psi / kappa per
   // rotation, while the forward stored psi with the scale of the forward
   // scaled forms.  Keeping <lam|P|psi> unscaled at every sweep boundary needs
@@ -772,6 +790,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
   for (int j = 0; j < d.nz; ++j) any_base |= S.zk[j] == -2;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
+    const int zp = zpt | zpattern((uint64_t)base, d);
     R tT = (R)0, tG = (R)0;
     if (active) {
       // all of this thread's loads of the tile in flight at once (asynchronous
@@ -786,26 +805,34 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       }
       cp_async_commit();
       cp_async_wait<0>();
-      for (int k = 0; k < nk; ++k) {
-        const int e = tid + k * NTHREADS;
-        const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        C l = tl[sw<R>(e)];
-        C q = tp[sw<R>(e)];
-        if (d.lam_undo == ENT_CZ && cz_negative(x)) l = cneg(l);
-        if (d.psi_undo == ENT_CZ && cz_negative(x)) q = cneg(q);
-        if (need_w) {
-          const R w = fma(l.x, q.y, -l.y * q.x);  // Im(conj(l) q)
-          tT += w;
+      const bool cz_l = d.lam_undo == ENT_CZ, cz_p = d.psi_undo == ENT_CZ;
+      if (need_w || cz_l || cz_p) {
+        for (int k = 0; k < nk; ++k) {
+          const int e = tid + k * NTHREADS;
+          const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
+          C l = tl[sw<R>(e)];
+          C q = tp[sw<R>(e)];
+          const bool neg = (cz_l || cz_p) && cz_negative(x);
+          if (cz_l && neg) {
+            l = cneg(l);
+            tl[sw<R>(e)] = l;
+          }
+          if (cz_p && neg) {
+            q = cneg(q);
+            tp[sw<R>(e)] = q;
+          }
+          if (need_w) {
+            const R w = fma(l.x, q.y, -l.y * q.x);  // Im(conj(l) q)
+            tT += w;
 #pragma unroll
-          for (int i = 0; i < 5; ++i)
-            if (((k >> i) & 1) && (S.zkmask >> i) & 1) Uk[i] += w;
-          if (d.gslot >= 0) {
-            const R cx = (R)(d.gcost == COST_INT ? d.cost_w0 * (double)p.cost_i[x] : p.cost_d[x]);
-            tG = fma(cx, w, tG);
+            for (int i = 0; i < 5; ++i)
+              if (((k >> i) & 1) && (S.zkmask >> i) & 1) Uk[i] += w;
+            if (d.gslot >= 0) {
+              const R cx = d.gcost == COST_INT ? w0r * (R)p.cost_i[x] : (R)p.cost_d[x];
+              tG = fma(cx, w, tG);
+            }
           }
         }
-        tl[sw<R>(e)] = l;
-        tp[sw<R>(e)] = q;
       }
     }
     if (d.nz > 0) {
@@ -838,9 +865,10 @@ __global__ void __launch_bounds__(NTHREADS) sweep_bwd_kernel(const __grid_consta
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        p.lam_out[x] = apply_diag<C>(tl[sw<R>(e)], x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true);
+        const int zpe = zp | S.zpk[k];
+        p.lam_out[x] = apply_diag<C>(tl[sw<R>(e)], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true);
         if (UNCOMPUTE)
-          p.psi_out[x] = cscale(apply_diag<C>(tp[sw<R>(e)], x, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold,
+          p.psi_out[x] = cscale(apply_diag<C>(tp[sw<R>(e)], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold,
                                               true),
                                 psi_mult);
       }
