@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--p", type=int, default=10, help="QAOA depth")
     ap.add_argument("--requests", type=int, default=120, help="serving: requests in the Poisson stream")
     ap.add_argument("--rate", type=float, default=0.0, help="serving: arrivals per second (0: saturate)")
+    ap.add_argument("--max-qubits", type=int, default=26, help="serving: cap of the request qubit counts")
     return ap.parse_args()
 
 
@@ -342,9 +343,11 @@ def run_qaoa(args):
         print(json.dumps(line))
 
 
-def serving_mix(seed, count):
-    """Config-5 request mix: 60% McClean n ~ U{8..26}, L ~ U{5..60}; 40% QAOA
-    3-regular MaxCut n ~ U{10..24} (even), p ~ U{1..6}; dtype per request."""
+def serving_mix(seed, count, max_qubits=26):
+    """Mixed request population: 60% McClean n ~ U{8..26}, L ~ U{5..60}; 40%
+    QAOA 3-regular MaxCut n ~ U{10..24} (even), p ~ U{1..6}; dtype per
+    request.  max_qubits caps both qubit ranges (the small-circuit share of
+    the same population)."""
     from qradient_gb300 import McClean, Qaoa
     from qradient_gb300.optimization_problems import MaxCut, random_regular_edges
 
@@ -354,7 +357,7 @@ def serving_mix(seed, count):
         dtype = "complex128" if rng.random() < 0.5 else "complex64"
         op = "grad" if rng.random() < 0.7 else "run"
         if rng.random() < 0.6:
-            n = int(rng.integers(8, 27))
+            n = int(rng.integers(8, min(26, max_qubits) + 1))
             L = int(rng.integers(5, 61))
             zz = np.full((n, n), None)
             for i in range(n - 1):
@@ -363,7 +366,7 @@ def serving_mix(seed, count):
                         grad_mode="uncompute")
             prm = rng.uniform(0, 2 * np.pi, (L, n))
         else:
-            n = int(rng.integers(5, 13)) * 2
+            n = int(rng.integers(5, min(12, max_qubits // 2) + 1)) * 2
             p = int(rng.integers(1, 7))
             c = Qaoa(n, MaxCut(n, edge_set=random_regular_edges(3, n, seed * 1000 + k)).to_observable(), p,
                      dtype=dtype, grad_mode="uncompute")
@@ -383,7 +386,7 @@ def run_serving(args):
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    reqs = serving_mix(args.seed + rank, args.requests)
+    reqs = serving_mix(args.seed + rank, args.requests, args.max_qubits)
     # plain per-call path: one request at a time through the public API
     def alone(c, prm, op):
         if isinstance(c, McClean):
@@ -401,7 +404,7 @@ def run_serving(args):
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
     plain = len(reqs) / plain_s
-    rate = args.rate if args.rate > 0 else 4.0 * plain  # saturating arrival rate
+    rate = args.rate if args.rate > 0 else 10.0 * plain  # saturating arrival rate
     rng = np.random.default_rng(args.seed + 7)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
     srv = Server(device=dev, streams=4)
@@ -420,9 +423,11 @@ def run_serving(args):
     line = {"metric": "served circuits/s (run + grad_run mix)", "value": value * world, "unit": "circuits/s",
             "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed f64/f32", "data": "synthetic Poisson stream",
-            "config": {"workload": "mixed request stream: 60%% McClean n~U{8..26} L~U{5..60}, 40%% QAOA 3-regular "
-                                   "n~U{10..24} p~U{1..6}, 70%% grad_run / 30%% run, dtype per request; "
-                                   "%d requests, Poisson rate %.1f/s" % (len(reqs), rate)},
+            "config": {"workload": "mixed request stream: 60%% McClean n~U{8..%d} L~U{5..60}, 40%% QAOA 3-regular "
+                                   "n~U{10..%d} p~U{1..6}, 70%% grad_run / 30%% run, dtype per request; "
+                                   "%d requests, Poisson rate %.1f/s" % (min(26, args.max_qubits),
+                                                                       2 * min(12, args.max_qubits // 2), len(reqs),
+                                                                       rate)},
             "latency": st, "plain_per_call_circuits_s": plain, "speedup_vs_plain": value / plain,
             "e2e": {"value": value * world, "unit": "circuits/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": None}, "clocks": clk}

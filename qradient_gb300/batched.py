@@ -39,10 +39,17 @@ CLUSTER_MAX = {_lib.QG_C64: 14, _lib.QG_C128: 13}
 MAX_COST = 511
 
 
+def _to_device(host, device):
+    """Host array -> device tensor without synchronising the current stream:
+    staged through pinned memory (whose block the host allocator keeps until
+    the copy has run) and copied asynchronously in stream order.  A plain
+    copy from pageable memory would wait for all earlier work on the stream."""
+    return torch.from_numpy(host).pin_memory().to(device, non_blocking=True)
+
+
 def _dev_bytes(arr, device):
     a = np.ascontiguousarray(arr)
-    t = torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).to(device)
-    return t
+    return _to_device(a.view(np.uint8).reshape(-1).copy(), device)
 
 
 class Batch:
@@ -84,21 +91,26 @@ class Batch:
 
     def finalize(self):
         dev = self.device
-        lib = _lib.load()
         total = sum(s["nparams"] for s in self._specs)
         B = len(self._specs)
-        self.params_flat = torch.zeros(max(total, 1), dtype=torch.float64, device=dev)
-        self.grads_flat = torch.zeros(max(total, 1), dtype=torch.float64, device=dev)
-        self.expec = torch.zeros(max(B, 1), dtype=torch.float64, device=dev)
-        self.params, self.grads = [], []
+        # initial parameters packed on the host and copied in one transfer
+        host = np.zeros(max(total, 1), dtype=np.float64)
         off = 0
         for s in self._specs:
             s["off"] = off
-            self.params.append(self.params_flat[off: off + s["nparams"]])
-            self.grads.append(self.grads_flat[off: off + s["nparams"]])
             if s["init"] is not None:
-                self.params[-1].copy_(torch.as_tensor(np.asarray(s["init"], dtype=np.float64)).reshape(-1))
+                init = s["init"]
+                if isinstance(init, torch.Tensor):
+                    init = init.detach().cpu().numpy()
+                host[off: off + s["nparams"]] = np.asarray(init, dtype=np.float64).reshape(-1)
             off += s["nparams"]
+        self.params_flat = _to_device(host, dev)
+        # every output slot is written by the kernels (a 2-CTA job clears its
+        # slots before adding to them), so no clearing is needed here
+        self.grads_flat = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+        self.expec = torch.empty(max(B, 1), dtype=torch.float64, device=dev)
+        self.params = [self.params_flat[s["off"]: s["off"] + s["nparams"]] for s in self._specs]
+        self.grads = [self.grads_flat[s["off"]: s["off"] + s["nparams"]] for s in self._specs]
         self._structures = {}
         self._build_groups()
         self.finalized = True
@@ -114,57 +126,97 @@ class Batch:
 
     def _build_groups(self):
         dev = self.device
-        # shared structure buffers, one per distinct circuit object
+        # shared structure buffers, one per distinct circuit object, packed
+        # into one device blob (one host-to-device copy for the batch)
         cache = self._structures
-        small, clus, big = [], [], []
+        self._upload_structures()
         single, cmax = SINGLE_MAX[self.dtype], CLUSTER_MAX[self.dtype]
         split = max(4, min(self.cluster_from, single + 1))
+        # job tables filled column by column (one numpy assignment per field)
+        cols = {k: [] for k in ("i", "kind", "n", "layers", "entangler", "placement", "nterms", "terms", "axes",
+                                "cost_nterms", "cost_maxabs", "cost_w0", "cost")}
+        big = []
         for i, s in enumerate(self._specs):
             c = s["circuit"]
-            key = id(c)
-            if key not in cache:
-                cache[key] = self._structure(c, s["kind"])
-            st = cache[key]
+            st = cache[id(c)]
             if c.qnum > cmax or st is None:
                 big.append(i)
                 continue
-            job = np.zeros(1, dtype=_JOB)
-            job["kind"] = s["kind"]
-            job["n"] = c.qnum
-            job["layers"] = c.lnum
-            job["entangler"] = _ENT[c.entangler] if s["kind"] == 0 else 0
-            job["placement"] = _PLACE[c.placement] if s["kind"] == 0 else 0
-            job["nterms"] = st["nterms"]
-            job["terms"] = st["terms"].data_ptr() if st["terms"] is not None else 0
-            job["axes"] = st["axes"].data_ptr() if st["axes"] is not None else 0
-            job["params"] = self.params[i].data_ptr()
-            job["expec"] = self.expec[i:i + 1].data_ptr()
-            job["grad"] = self.grads[i].data_ptr() if self.want_grad else 0
-            job["cost_nterms"] = st["cost_nterms"]
-            job["cost_maxabs"] = st["cost_maxabs"]
-            job["cost_w0"] = st["cost_w0"]
-            job["cost"] = st["cost"].data_ptr() if st["cost"] is not None else 0
-            (small if c.qnum < split else clus).append((c.qnum, job))
-        self._keep = list(cache.values())
+            mc = s["kind"] == 0
+            for k, v in (("i", i), ("kind", s["kind"]), ("n", c.qnum), ("layers", c.lnum),
+                         ("entangler", _ENT[c.entangler] if mc else 0), ("placement", _PLACE[c.placement] if mc else 0),
+                         ("nterms", st["nterms"]), ("terms", st["terms"]), ("axes", st["axes"]),
+                         ("cost_nterms", st["cost_nterms"]), ("cost_maxabs", st["cost_maxabs"]),
+                         ("cost_w0", st["cost_w0"]), ("cost", st["cost"])):
+                cols[k].append(v)
+        idx = np.asarray(cols["i"], dtype=np.int64)
+        qn = np.asarray(cols["n"], dtype=np.int64)
+        offs = np.asarray([self._specs[i]["off"] for i in idx], dtype=np.uint64)
+        pbase, gbase, ebase = self.params_flat.data_ptr(), self.grads_flat.data_ptr(), self.expec.data_ptr()
         self._groups = []
-        for cl, jobs in ((1, small), (2, clus)):
-            if not jobs:
+        for cl, sel in ((1, qn < split), (2, qn >= split)):
+            nj = int(sel.sum())
+            if nj == 0:
                 continue
-            arr = np.concatenate([j for _, j in jobs])
-            maxq = max(q for q, _ in jobs)
-            ws = torch.zeros(256, dtype=torch.uint8, device=dev)
-            self._groups.append((cl, _dev_bytes(arr, dev), len(jobs), maxq, ws))
+            arr = np.zeros(nj, dtype=_JOB)
+            for k in ("kind", "n", "layers", "entangler", "placement", "nterms", "terms", "axes", "cost_nterms",
+                      "cost_maxabs", "cost_w0", "cost"):
+                arr[k] = np.asarray(cols[k])[sel]
+            arr["params"] = pbase + 8 * offs[sel]
+            arr["expec"] = ebase + 8 * idx[sel].astype(np.uint64)
+            arr["grad"] = gbase + 8 * offs[sel] if self.want_grad else 0
+            maxq = int(qn[sel].max())
+            ws = torch.empty(256, dtype=torch.uint8, device=dev)  # job counter, cleared by qg_batch_launch
+            self._groups.append((cl, _dev_bytes(arr, dev), nj, maxq, ws))
         self._big = big
 
+    def _upload_structures(self):
+        """Host arrays of every circuit not yet uploaded, packed 16-byte
+        aligned into one buffer and copied to the device at once; the cache
+        then holds device addresses."""
+        pending, blobs, size, seen = [], [], 0, set()
+        for s in self._specs:
+            c = s["circuit"]
+            if id(c) in self._structures or id(c) in seen:
+                continue
+            seen.add(id(c))
+            st = self._structure(c, s["kind"])
+            if st is None:
+                self._structures[id(c)] = None  # runs on the sweep path
+                continue
+            offs = {}
+            for key in ("terms", "axes", "cost"):
+                a = st[key]
+                if a is None:
+                    continue
+                b = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
+                size = (size + 15) & ~15
+                offs[key] = size
+                blobs.append((size, b))
+                size += b.size
+            pending.append((c, st, offs))
+        if not pending:
+            return
+        host = np.zeros(max(size, 16), dtype=np.uint8)
+        for o, b in blobs:
+            host[o:o + b.size] = b
+        buf = _to_device(host, self.device)
+        self._blobs = getattr(self, "_blobs", []) + [buf]
+        base = buf.data_ptr()
+        for c, st, offs in pending:
+            for key in ("terms", "axes", "cost"):
+                st[key] = base + offs[key] if key in offs else 0
+            self._structures[id(c)] = st
+
     def _structure(self, c, kind):
-        dev = self.device
+        """Host-side structure arrays of one circuit (uploaded by the caller)."""
         kindv, q0, q1, w = c.observable.terms
         terms = np.zeros(len(kindv), dtype=_TERM)
         terms["kind"], terms["q0"], terms["q1"], terms["w"] = kindv, q0, q1, w
-        st = {"nterms": len(kindv), "terms": _dev_bytes(terms, dev) if len(kindv) else None, "axes": None,
+        st = {"nterms": len(kindv), "terms": terms if len(kindv) else None, "axes": None,
               "cost": None, "cost_nterms": 0, "cost_maxabs": 0, "cost_w0": 1.0}
         if kind == 0:
-            st["axes"] = torch.as_tensor(np.asarray(c.axes, dtype=np.int8).reshape(-1), device=dev)
+            st["axes"] = np.asarray(c.axes, dtype=np.int8).reshape(-1)
         else:
             lib = _lib.load()
             out = np.zeros(600, dtype=_COST)
@@ -176,7 +228,7 @@ class Batch:
                                             ctypes.byref(w0), ctypes.byref(maxabs))
             if status != _lib.QG_OK or maxabs.value > MAX_COST:
                 return None  # not representable in the batched kernel: sweep path
-            st["cost"] = _dev_bytes(out[: nout.value], dev) if nout.value else None
+            st["cost"] = out[: nout.value].copy() if nout.value else None
             st["cost_nterms"], st["cost_maxabs"], st["cost_w0"] = nout.value, maxabs.value, w0.value
         return st
 

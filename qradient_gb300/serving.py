@@ -11,9 +11,10 @@ dtype) arrive over time.  Each scheduling round:
    that fit the shared-memory kernel need only their parameters and
    outputs);
 3. admitted small requests are packed into one batched persistent launch
-   (``qg_batch_launch``), each admitted large request gets its own stream
-   running the sweep kernels.  Work from different rounds overlaps on the
-   device: a round never waits for earlier launches.
+   (``qg_batch_launch``) on the next of a few batch streams, each admitted
+   large request gets its own stream running the sweep kernels.  Work from
+   different rounds overlaps on the device: a round never waits for earlier
+   launches, and host-to-device copies are asynchronous (pinned staging).
 
 Results are identical to running the request alone (same kernels, same
 reduction order); ``tests/test_gpu_serving.py`` checks this.
@@ -65,7 +66,7 @@ class Server:
     """Admission by device-memory footprint, batched small requests, one
     stream per large request (up to ``streams`` concurrently)."""
 
-    def __init__(self, device=None, hbm_budget=None, streams=4, max_batch=4096):
+    def __init__(self, device=None, hbm_budget=None, streams=4, max_batch=4096, batch_streams=4):
         self.device = _native.require_cuda(device)
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info(self.device)
@@ -78,7 +79,10 @@ class Server:
         self.finished = []
         self.streams = [torch.cuda.Stream(self.device) for _ in range(streams)]
         self.stream_busy = [None] * streams
-        self.batch_stream = torch.cuda.Stream(self.device)
+        # batches of consecutive rounds go to different streams: a round's
+        # batch often has fewer jobs than the GPU has SMs, so batches overlap
+        self.batch_streams = [torch.cuda.Stream(self.device) for _ in range(batch_streams)]
+        self._next_batch_stream = 0
         self._rid = 0
 
     # ------------------------------------------------------------ interface
@@ -113,12 +117,22 @@ class Server:
                 still.append(item)
                 continue
             now = time.perf_counter()
-            for r in reqs:
-                r.expec = float(r._e.item())
-                if r.op == "grad":
-                    shape = (r.circuit.lnum, r.circuit.qnum) if r.circuit.__class__.__name__ == "McClean" else (
-                        r.circuit.lnum, 2)
-                    r.grad = r._g.cpu().numpy().reshape(shape)
+            if isinstance(keep, Batch):
+                # one device-to-host copy per output array of the batch
+                E = keep.expec.cpu().numpy()
+                G = keep.grads_flat.cpu().numpy() if keep.want_grad else None
+            for k, r in enumerate(reqs):
+                shape = (r.circuit.lnum, r.circuit.qnum) if r.circuit.__class__.__name__ == "McClean" else (
+                    r.circuit.lnum, 2)
+                if isinstance(keep, Batch):
+                    r.expec = float(E[k])
+                    if r.op == "grad":
+                        off = keep._specs[k]["off"]
+                        r.grad = G[off: off + keep._specs[k]["nparams"]].copy().reshape(shape)
+                else:
+                    r.expec = float(r._e.item())
+                    if r.op == "grad":
+                        r.grad = r._g.cpu().numpy().reshape(shape)
                 r.t_done = now
                 self.in_use -= r.footprint
                 r._e = r._g = None
@@ -152,18 +166,17 @@ class Server:
         by_dtype = collections.defaultdict(list)
         for r in reqs:
             by_dtype[r.dtype].append(r)
-        with torch.cuda.stream(self.batch_stream):
+        st = self.batch_streams[self._next_batch_stream]
+        self._next_batch_stream = (self._next_batch_stream + 1) % len(self.batch_streams)
+        with torch.cuda.stream(st):
             for dt, rs in by_dtype.items():
                 b = Batch(device=self.device, dtype=dt, grad=any(r.op == "grad" for r in rs), use_graph=False)
                 for r in rs:
                     b.add(r.circuit, params=r.params.reshape(-1))
                 b.finalize()
                 b.execute()
-                for k, r in enumerate(rs):
-                    r._e = b.expec[k:k + 1]
-                    r._g = b.grads[k]
                 ev = torch.cuda.Event()
-                ev.record(self.batch_stream)
+                ev.record(st)
                 self.inflight.append((ev, rs, b))
 
     def _launch_large(self, r):
