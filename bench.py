@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--requests", type=int, default=120, help="serving: requests in the Poisson stream")
     ap.add_argument("--rate", type=float, default=0.0, help="serving: arrivals per second (0: saturate)")
     ap.add_argument("--max-qubits", type=int, default=26, help="serving: cap of the request qubit counts")
+    ap.add_argument("--streams", type=int, default=8, help="serving: concurrent large requests (one stream each)")
     return ap.parse_args()
 
 
@@ -407,7 +408,7 @@ def run_serving(args):
     rate = args.rate if args.rate > 0 else 10.0 * plain  # saturating arrival rate
     rng = np.random.default_rng(args.seed + 7)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
-    srv = Server(device=dev, streams=4)
+    srv = Server(device=dev, streams=args.streams)
     # warm-up round (kernel attributes, lazy module loading)
     srv.serve([(0.0, c, prm, op, dt) for c, prm, op, dt in reqs[:4]])
     srv.finished.clear()

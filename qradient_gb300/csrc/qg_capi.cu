@@ -73,6 +73,11 @@ struct qg_circuit {
   int tune_tile_bits[2] = {0, 0};
   int tune_ctas[2] = {0, 0};
   int tune_flags[2] = {0, 0};  // QG_TUNE_* bits
+  // plans (sweep program, workspace layout, observable launches) built on
+  // first use per (device, dtype, op, start state) and reused: the host
+  // work of a call is then the launches alone
+  mutable std::mutex plan_mu;
+  mutable std::vector<std::pair<int, std::shared_ptr<const void>>> plans;
   IntTermList* iterms = nullptr;
   RealTermList* rterms = nullptr;
   ~qg_circuit() {
@@ -451,6 +456,46 @@ int check_circuit(const qg_circuit* c) {
   return QG_OK;
 }
 
+std::vector<ObsDesc> build_obs(const qg_circuit* c, const Program& P, bool grad, bool store,
+                               const std::vector<Term>* terms);
+
+struct Plan {
+  Program P;
+  WsLayout W;
+  std::vector<ObsDesc> obs;  // observable launches (lam stored for gradient ops)
+};
+
+// The cached plan of (current device, dtype, op, with_ini); built on first use.
+int get_plan(const qg_circuit* c, int dtype, int op, bool with_ini, std::shared_ptr<const Plan>& out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  const int key = ((dev * 2 + dtype) * 4 + op) * 2 + (with_ini ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lock(c->plan_mu);
+    for (const auto& kv : c->plans)
+      if (kv.first == key) {
+        out = std::static_pointer_cast<const Plan>(kv.second);
+        return QG_OK;
+      }
+  }
+  auto plan = std::make_shared<Plan>();
+  if (int s = build_program(c, dtype, with_ini, plan->P)) return s;
+  plan->W = ws_layout(c, dtype, op, plan->P);
+  plan->obs = build_obs(c, plan->P, op != QG_OP_RUN, op != QG_OP_RUN, nullptr);
+  std::lock_guard<std::mutex> lock(c->plan_mu);
+  c->plans.emplace_back(key, plan);
+  out = plan;
+  return QG_OK;
+}
+
+void clear_plans(const qg_circuit* c) {
+  std::lock_guard<std::mutex> lock(c->plan_mu);
+  c->plans.clear();
+}
+
 int build_cost(const qg_circuit* c, char* ws, const WsLayout& W, cudaStream_t st) {
   if (c->kind != 1) return QG_OK;
   const int grid = sm_count() * 8;
@@ -465,35 +510,31 @@ int build_cost(const qg_circuit* c, char* ws, const WsLayout& W, cudaStream_t st
 // Observable passes: lam = O psi (store) and the expectation partial sums.
 // `terms` replaces the circuit's observable (the sampled component of
 // grad_run_with_component_sampling); null means the circuit's own terms.
-template <typename R>
-int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, bool grad, const typename C2T<R>::T* psi,
-                   typename C2T<R>::T* lam, char* ws, cudaStream_t st, const std::vector<Term>* terms = nullptr) {
+// Built on the host once per plan; launched by run_observable.
+std::vector<ObsDesc> build_obs(const qg_circuit* c, const Program& P, bool grad, bool store,
+                               const std::vector<Term>* terms) {
   const int n = c->n;
-  double* partials = (double*)(ws + W.partials);
-  const int32_t* ci = (const int32_t*)(ws + W.cost);
-  const double* cd = (const double*)(ws + W.cost);
-  ObsDesc* d = new (std::nothrow) ObsDesc;
-  if (!d) return fail(QG_ERR_HOST_MEMORY, "host allocation failed");
-  std::unique_ptr<ObsDesc> guard(d);
+  std::vector<ObsDesc> out;
   const Layout& lay = P.lay;
   const int eslot0 = P.nslots;
-  auto fill = [&](int s) {
+  auto fresh = [&](int s) {
+    out.emplace_back();
+    ObsDesc* d = &out.back();
     memset(d, 0, sizeof *d);
     d->n = n;
     d->t = (int)lay.tiles[s].size();
     for (size_t i = 0; i < lay.tiles[s].size(); ++i) d->bits[i] = (uint8_t)lay.tiles[s][i];
-    d->store = lam != nullptr;
+    d->store = store;
     d->pre = P.obs_pre;
+    return d;
   };
   if (c->kind == 1 && grad) {
     // lam = C psi with the classical cost (qaoa.py:56-57)
-    fill(0);
+    ObsDesc* d = fresh(0);
     d->cost = (int8_t)c->cost_kind;
     d->cost_w0 = c->cost_w0;
     d->eslot = eslot0;
-    ProfScope ps(2, st);
-    QG_CUDA(launch_observable<R>(*d, psi, lam, ci, cd, partials, W.G, W.G, st));
-    return QG_OK;
+    return out;
   }
   // diagonal terms sorted by weight, then X/Y terms of tile A
   std::vector<Term> diag, xy;
@@ -501,7 +542,7 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
   std::stable_sort(diag.begin(), diag.end(), [](const Term& a, const Term& b) { return a.w < b.w; });
   int es = 0;
   for (size_t s = 0; s < lay.tiles.size(); ++s) {
-    fill((int)s);
+    ObsDesc* d = fresh((int)s);
     int k = 0;
     if (s == 0) {
       for (const auto& tm : diag) {
@@ -530,11 +571,25 @@ int run_observable(const qg_circuit* c, const Program& P, const WsLayout& W, boo
       ++nxy;
     }
     d->nxy = nxy;
-    if (s > 0 && nxy == 0) continue;
+    if (s > 0 && nxy == 0) {
+      out.pop_back();
+      continue;
+    }
     d->accumulate = s > 0;
     d->eslot = eslot0 + es++;
+  }
+  return out;
+}
+
+template <typename R>
+int run_observable(const std::vector<ObsDesc>& obs, const WsLayout& W, const typename C2T<R>::T* psi,
+                   typename C2T<R>::T* lam, char* ws, cudaStream_t st) {
+  double* partials = (double*)(ws + W.partials);
+  const int32_t* ci = (const int32_t*)(ws + W.cost);
+  const double* cd = (const double*)(ws + W.cost);
+  for (const ObsDesc& d : obs) {
     ProfScope ps(2, st);
-    QG_CUDA(launch_observable<R>(*d, psi, lam, ci, cd, partials, W.G, W.G, st));
+    QG_CUDA(launch_observable<R>(d, psi, lam, ci, cd, partials, W.G, W.G, st));
   }
   return QG_OK;
 }
@@ -578,17 +633,18 @@ template <typename R>
 int do_run(const qg_circuit* c, const double* params, const void* ini, char* ws, size_t wsb, double* expec,
            void* state_out, cudaStream_t st, int dtype) {
   using C = typename C2T<R>::T;
-  Program P;
-  int s = build_program(c, dtype, ini != nullptr, P);
+  std::shared_ptr<const Plan> plan;
+  int s = get_plan(c, dtype, QG_OP_RUN, ini != nullptr, plan);
   if (s) return s;
-  WsLayout W = ws_layout(c, dtype, QG_OP_RUN, P);
+  const Program& P = plan->P;
+  const WsLayout& W = plan->W;
   if (wsb < W.total) return fail(QG_ERR_WORKSPACE, "workspace %zu bytes < %zu needed", wsb, W.total);
   s = build_cost(c, ws, W, st);
   if (s) return s;
   const C* fin = nullptr;
   s = forward<R>(c, P, W, params, ini, false, ws, st, &fin);
   if (s) return s;
-  s = run_observable<R>(c, P, W, false, fin, nullptr, ws, st);
+  s = run_observable<R>(plan->obs, W, fin, nullptr, ws, st);
   if (s) return s;
   QG_CUDA(launch_finalize((double*)(ws + W.partials), W.G, 0, c->n, 0, P.nslots, W.neslots, expec, nullptr, st));
   if (state_out) QG_CUDA(cudaMemcpyAsync(state_out, fin, W.state_bytes, cudaMemcpyDeviceToDevice, st));
@@ -601,10 +657,11 @@ template <typename R>
 int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, char* ws, size_t wsb, double* expec,
             double* grad, cudaStream_t st, int dtype, int component = -1) {
   using C = typename C2T<R>::T;
-  Program P;
-  int s = build_program(c, dtype, ini != nullptr, P);
+  std::shared_ptr<const Plan> plan;
+  int s = get_plan(c, dtype, op, ini != nullptr, plan);
   if (s) return s;
-  WsLayout W = ws_layout(c, dtype, op, P);
+  const Program& P = plan->P;
+  const WsLayout& W = plan->W;
   if (wsb < W.total) return fail(QG_ERR_WORKSPACE, "workspace %zu bytes < %zu needed", wsb, W.total);
   const bool history = op == QG_OP_GRAD_HISTORY;
   QG_CUDA(cudaMemsetAsync(ws + W.partials, 0, (size_t)(P.nslots + W.neslots) * W.G * sizeof(double), st));
@@ -623,11 +680,11 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
     // overwritten by the full-observable pass, which writes at least the
     // same slots, so E stays <psi|O|psi> (mc_clean.py:99-100)
     const std::vector<Term> one(1, c->terms[component]);
-    s = run_observable<R>(c, P, W, true, fin, lbuf[lc], ws, st, &one);
+    s = run_observable<R>(build_obs(c, P, true, true, &one), W, fin, lbuf[lc], ws, st);
     if (s) return s;
-    s = run_observable<R>(c, P, W, false, fin, nullptr, ws, st);
+    s = run_observable<R>(build_obs(c, P, false, false, nullptr), W, fin, nullptr, ws, st);
   } else {
-    s = run_observable<R>(c, P, W, true, fin, lbuf[lc], ws, st);
+    s = run_observable<R>(plan->obs, W, fin, lbuf[lc], ws, st);
   }
   if (s) return s;
   SweepPtrs<R> p;
@@ -861,11 +918,10 @@ int qg_workspace_size(const qg_circuit* c, int dtype, int op, size_t* bytes) {
   if (!bytes) return fail(QG_ERR_INVALID, "null output");
   if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
   if (op < QG_OP_RUN || op > QG_OP_GRAD_UNCOMPUTE) return fail(QG_ERR_INVALID, "unknown op %d", op);
-  Program P;
   // the start state adds a fixed Ry layer (McClean) when given; size for the larger case
-  int s = build_program(c, dtype, c->kind == 0, P);
-  if (s) return s;
-  *bytes = ws_layout(c, dtype, op, P).total;
+  std::shared_ptr<const Plan> plan;
+  if (int s = get_plan(c, dtype, op, c->kind == 0, plan)) return s;
+  *bytes = plan->W.total;
   return QG_OK;
 }
 
@@ -973,6 +1029,7 @@ int qg_set_tuning(qg_circuit* c, int dtype, int tile_bits, int ctas_per_sm, int 
   c->tune_tile_bits[dtype] = tile_bits;
   c->tune_ctas[dtype] = ctas_per_sm;
   c->tune_flags[dtype] = flags;
+  clear_plans(c);
   return QG_OK;
 }
 
@@ -980,10 +1037,10 @@ int qg_get_tuning(const qg_circuit* c, int dtype, int* tile_bits, int* ctas_per_
   if (int s = check_circuit(c)) return s;
   if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
   if (!tile_bits || !ctas_per_sm) return fail(QG_ERR_INVALID, "null output");
-  Program P;
-  if (int s = build_program(c, dtype, false, P)) return s;
-  WsLayout W = ws_layout(c, dtype, QG_OP_GRAD_HISTORY, P);
-  *tile_bits = P.lay.t;
+  std::shared_ptr<const Plan> plan;
+  if (int s = get_plan(c, dtype, QG_OP_GRAD_HISTORY, false, plan)) return s;
+  const WsLayout& W = plan->W;
+  *tile_bits = plan->P.lay.t;
   const int sms = sm_count();
   *ctas_per_sm = sms > 0 ? (W.G + sms - 1) / sms : W.G;
   if (flags) *flags = W.fwd_pipe ? QG_TUNE_FWD_PIPELINED : QG_TUNE_FWD_PLAIN;

@@ -7,6 +7,9 @@
 //   observable         physical_components/observable.py:34-73, base.py:17-20
 //   McClean grad_run   circuit_logic/mc_clean.py:47-78
 //   QAOA grad_run      circuit_logic/qaoa.py:40-70
+#include <atomic>
+#include <mutex>
+
 #include "qg_internal.cuh"
 #include "qg_kernels.h"
 
@@ -1125,24 +1128,60 @@ static size_t sweep_smem(const SweepDesc& d, bool bwd, bool pipe = false) {
   return s;
 }
 
+// Raise the dynamic shared-memory limit of every kernel of the sweep path
+// to what the device allows next to its static shared memory, once per
+// device, so that launches need no attribute call.
+static cudaError_t set_smem_limit(const void* fn, int optin) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, fn);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes);
+}
+
+cudaError_t prepare_sweep_kernels() {
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> ready[kMaxDev];
+  static std::mutex mu;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  if (ready[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(mu);
+  if (ready[dev].load(std::memory_order_relaxed)) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  const void* fns[] = {(const void*)sweep_fwd_kernel<double>,          (const void*)sweep_fwd_kernel<float>,
+                       (const void*)sweep_fwd_pipe_kernel<double>,     (const void*)sweep_fwd_pipe_kernel<float>,
+                       (const void*)sweep_bwd_kernel<double, false>,   (const void*)sweep_bwd_kernel<double, true>,
+                       (const void*)sweep_bwd_kernel<float, false>,    (const void*)sweep_bwd_kernel<float, true>,
+                       (const void*)observable_kernel<double>,         (const void*)observable_kernel<float>};
+  for (const void* fn : fns) {
+    e = set_smem_limit(fn, optin);
+    if (e != cudaSuccess) return e;
+  }
+  ready[dev].store(1, std::memory_order_release);
+  return cudaSuccess;
+}
+
 template <typename R>
 int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe) {
   const size_t smem = sweep_smem<R>(d, bwd, pipe && !bwd);
   int blocks = 0;
-  cudaError_t e;
-  if (!bwd && pipe) {
-    cudaFuncSetAttribute(sweep_fwd_pipe_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_pipe_kernel<R>, NTHREADS, smem);
-  } else if (!bwd) {
-    cudaFuncSetAttribute(sweep_fwd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_kernel<R>, NTHREADS, smem);
-  } else if (uncompute) {
-    cudaFuncSetAttribute(sweep_bwd_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, true>, NTHREADS, smem);
-  } else {
-    cudaFuncSetAttribute(sweep_bwd_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, false>, NTHREADS, smem);
+  cudaError_t e = prepare_sweep_kernels();
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
   }
+  if (!bwd && pipe)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_pipe_kernel<R>, NTHREADS, smem);
+  else if (!bwd)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_kernel<R>, NTHREADS, smem);
+  else if (uncompute)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, true>, NTHREADS, smem);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, false>, NTHREADS, smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -1155,34 +1194,25 @@ template int sweep_ctas_per_sm<float>(const SweepDesc&, bool, bool, bool);
 
 template <typename R>
 cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe) {
+  cudaError_t e = prepare_sweep_kernels();
+  if (e != cudaSuccess) return e;
   if (pipe && d.start == START_LOAD) {
-    const size_t smem = sweep_smem<R>(d, false, true);
-    cudaError_t e =
-        cudaFuncSetAttribute(sweep_fwd_pipe_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    sweep_fwd_pipe_kernel<R><<<grid, NTHREADS, smem, st>>>(d, p);
+    sweep_fwd_pipe_kernel<R><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
     return cudaGetLastError();
   }
-  const size_t smem = sweep_smem<R>(d, false);
-  cudaError_t e = cudaFuncSetAttribute(sweep_fwd_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  sweep_fwd_kernel<R><<<grid, NTHREADS, smem, st>>>(d, p);
+  sweep_fwd_kernel<R><<<grid, NTHREADS, sweep_smem<R>(d, false), st>>>(d, p);
   return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st) {
   const size_t smem = sweep_smem<R>(d, true);
-  cudaError_t e;
-  if (uncompute) {
-    e = cudaFuncSetAttribute(sweep_bwd_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+  cudaError_t e = prepare_sweep_kernels();
+  if (e != cudaSuccess) return e;
+  if (uncompute)
     sweep_bwd_kernel<R, true><<<grid, NTHREADS, smem, st>>>(d, p);
-  } else {
-    e = cudaFuncSetAttribute(sweep_bwd_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+  else
     sweep_bwd_kernel<R, false><<<grid, NTHREADS, smem, st>>>(d, p);
-  }
   return cudaGetLastError();
 }
 
@@ -1192,7 +1222,7 @@ cudaError_t launch_observable(const ObsDesc& d, const typename C2T<R>::T* psi, t
                               cudaStream_t st) {
   using C = typename C2T<R>::T;
   const size_t smem = ((size_t)1 << d.t) * sizeof(C);
-  cudaError_t e = cudaFuncSetAttribute(observable_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   observable_kernel<R><<<grid, NTHREADS, smem, st>>>(d, psi, lam, cost_i, cost_d, partials, G);
   return cudaGetLastError();

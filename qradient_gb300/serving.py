@@ -66,7 +66,7 @@ class Server:
     """Admission by device-memory footprint, batched small requests, one
     stream per large request (up to ``streams`` concurrently)."""
 
-    def __init__(self, device=None, hbm_budget=None, streams=4, max_batch=4096, batch_streams=4):
+    def __init__(self, device=None, hbm_budget=None, streams=8, max_batch=4096, batch_streams=4):
         self.device = _native.require_cuda(device)
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info(self.device)
