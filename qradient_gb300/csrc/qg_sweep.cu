@@ -991,16 +991,22 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
           } else if (d.cost == COST_REAL) {
             dv = cost_d[x];
           } else {
-            // integer sign sums per run of equal weights, one multiply per run
-            int cnt = 0;
-            for (int i = 0; i < d.ndiag; ++i) {
-              const ObsTerm& tm = d.term[i];
-              const uint64_t m = (1ull << tm.b0) | (tm.kind == 3 ? (1ull << tm.b1) : 0ull);
-              cnt += 1 - 2 * (__popcll(x & m) & 1);
-              if (tm.endgrp) {
-                dv = fma(tm.w, (double)cnt, dv);
-                cnt = 0;
-              }
+            // integer sign sums per run of equal weights, one multiply per
+            // run: the inner loop is integer only, so the compiler cannot
+            // predicate the double multiply into every term
+            int i = 0;
+            while (i < d.ndiag) {
+              int cnt = 0;
+              bool last;
+              double w;
+              do {
+                const ObsTerm& tm = d.term[i++];
+                const uint64_t m = (1ull << tm.b0) | (tm.kind == 3 ? (1ull << tm.b1) : 0ull);
+                cnt += 1 - 2 * (__popcll(x & m) & 1);
+                last = tm.endgrp;
+                w = tm.w;
+              } while (!last && i < d.ndiag);
+              dv = fma(w, (double)cnt, dv);
             }
           }
           lx = dv * (double)v.x;
