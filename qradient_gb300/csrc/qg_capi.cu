@@ -378,6 +378,10 @@ struct WsLayout {
   int G = 1, grid_fwd = 1;
   int neslots = 1;
   bool fwd_pipe = false;  // double-buffered forward sweeps
+  // per-sweep grids from each sweep's own occupancy (its phase table sets
+  // its shared memory); backward grids never exceed G, the width of the
+  // partial-sum rows (entries of blocks a sweep does not launch stay zero)
+  std::vector<int> grid_fwd_k, grid_bwd_k;
 };
 
 int obs_sweeps_needed(const qg_circuit* c, const Layout& lay, bool grad) {
@@ -423,6 +427,34 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
   }
   w.G = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_bwd);
   w.grid_fwd = (int)std::min<int64_t>(ntiles, (int64_t)sms * per_fwd);
+  {
+    // occupancy per distinct shared-memory footprint (phase-table size, cost table)
+    std::vector<std::pair<int64_t, std::pair<int, int>>> memo;
+    for (const auto& d : P.sweeps) {
+      const int64_t key = ((int64_t)d.nz << 32) | ((int64_t)(d.cost == COST_INT ? 1 : 0) << 31) | d.cost_maxabs;
+      int pf = -1, pb = -1;
+      for (const auto& mm : memo)
+        if (mm.first == key) {
+          pf = mm.second.first;
+          pb = mm.second.second;
+        }
+      if (pf < 0) {
+        pf = dtype == QG_C128 ? sweep_ctas_per_sm<double>(d, false, false, pipe)
+                              : sweep_ctas_per_sm<float>(d, false, false, pipe);
+        pb = dtype == QG_C128 ? sweep_ctas_per_sm<double>(d, true, unc) : sweep_ctas_per_sm<float>(d, true, unc);
+        if (tuned > 0) {
+          pf = std::min(pf, tuned);
+          pb = std::min(pb, tuned);
+        } else {
+          pb = env_int("QG_CTAS_PER_SM", pb);
+        }
+        memo.push_back({key, {pf, pb}});
+      }
+      w.grid_fwd_k.push_back((int)std::min<int64_t>(ntiles, (int64_t)sms * pf));
+      w.grid_bwd_k.push_back((int)std::min<int64_t>(ntiles, (int64_t)sms * pb));
+    }
+    for (int g : w.grid_bwd_k) w.G = std::max(w.G, g);
+  }
   w.neslots = obs_sweeps_needed(c, P.lay, op != QG_OP_RUN);
   const int m = (int)P.sweeps.size();
   w.pingpong = P.obs_pre == ENT_CNOT;
@@ -622,7 +654,7 @@ int forward(const qg_circuit* c, const Program& P, const WsLayout& W, const doub
     p.psi_in = in;
     p.psi_out = out;
     ProfScope ps(0, st);
-    QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd, st, W.fwd_pipe));
+    QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd_k[k], st, W.fwd_pipe));
     in = out;
   }
   *final_state = in;
@@ -713,7 +745,7 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
       p.psi_out = pbuf[pc];
     }
     ProfScope ps(1, st);
-    QG_CUDA(launch_sweep_bwd<R>(d, p, !history, W.G, st));
+    QG_CUDA(launch_sweep_bwd<R>(d, p, !history, W.grid_bwd_k[k], st));
   }
   C* lam = lbuf[lc];
   if (c->kind == 1 && c->L > 0) {

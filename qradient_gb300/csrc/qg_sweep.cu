@@ -260,8 +260,28 @@ struct SetupShared {
   int zpk[32];         // Z-table index bits contributed by offhi[k]
   uint8_t outside[QMAX];
   double startP[QMAX + 1];
-  double red[NTHREADS / 32][RS_N];
+  // complex64 kernels keep their per-tile sums and rotation multipliers in
+  // float: a double instruction, even on one lane, holds the FP64 pipe
+  // (2 lanes per clock) for 16 cycles.  A kernel uses one of the two arrays.
+  union {
+    double red[NTHREADS / 32][RS_N];
+    float redf[NTHREADS / 32][RS_N];
+  };
+  float uf[TMAX];
 };
+
+// this warp's partial-sum slot in the kernel's own precision
+template <typename R>
+__device__ __forceinline__ void red_slot_add(SetupShared& S, int w, int slot, R v) {
+  if (sizeof(R) == 4)
+    S.redf[w][slot] += (float)v;
+  else
+    S.red[w][slot] += (double)v;
+}
+template <typename R>
+__device__ __forceinline__ double red_slot(const SetupShared& S, int w, int slot) {
+  return sizeof(R) == 4 ? (double)S.redf[w][slot] : S.red[w][slot];
+}
 
 // Deposit the low bits of v into the listed bit positions.
 __device__ __forceinline__ int64_t deposit(int64_t v, const uint8_t* bits, int nb) {
@@ -282,6 +302,7 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
     int f;
     double k;
     S.u[tid] = rot_form(angle_of(d.xy[tid].a, params), &f, &k);
+    S.uf[tid] = (float)S.u[tid];
     S.form[tid] = f;
     S.kappa[tid] = k;
   }
@@ -304,7 +325,7 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
     }
     S.zkmask = m;
   }
-  for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;
+  for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;  // clears both views
   if (t > 8) {
     for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) {
       S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
@@ -421,16 +442,16 @@ __device__ __forceinline__ void red_add3(SetupShared& S, int slot0, const R* acc
   k += __shfl_xor_sync(full, k, 1);
   // lanes 0-7: v0, 8-15: v1, 16-23: v2, 24-31: v3
   const int w = threadIdx.x >> 5;
-  if (lane == 0) S.red[w][slot0] += (double)k;
-  if (G > 1 && lane == 8) S.red[w][slot0 + 1] += (double)k;
-  if (G > 2 && lane == 16) S.red[w][slot0 + 2] += (double)k;
+  if (lane == 0) red_slot_add<R>(S, w, slot0, k);
+  if (G > 1 && lane == 8) red_slot_add<R>(S, w, slot0 + 1, k);
+  if (G > 2 && lane == 16) red_slot_add<R>(S, w, slot0 + 2, k);
 }
 
 // add a per-thread value into this warp's reduction slot
 template <typename R>
 __device__ __forceinline__ void red_add(SetupShared& S, int slot, R v) {
   v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) S.red[threadIdx.x >> 5][slot] += (double)v;
+  if ((threadIdx.x & 31) == 0) red_slot_add<R>(S, threadIdx.x >> 5, slot, v);
 }
 
 // ------------------------------------------------------------ gate groups
@@ -450,7 +471,7 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
     b[i] = d.xy[g0 + i].lbit;
     ax[i] = d.xy[g0 + i].axis;
     fm[i] = S.form[g0 + i];
-    uu[i] = (R)S.u[g0 + i];
+    uu[i] = sizeof(R) == 4 ? (R)S.uf[g0 + i] : (R)S.u[g0 + i];
   }
   const int ntask = tsize >> G;
   for (int tk = threadIdx.x; tk < ntask; tk += NTHREADS) {
@@ -845,7 +866,7 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
         const R tot = warp_sum(tT);
         if ((tid & 31) == 0) {
           for (int j = 0; j < d.nz; ++j)
-            if (S.zk[j] == -2 && ((base >> d.z[j].gbit) & 1)) S.red[tid >> 5][RS_Z + j] += (double)tot;
+            if (S.zk[j] == -2 && ((base >> d.z[j].gbit) & 1)) red_slot_add<R>(S, tid >> 5, RS_Z + j, tot);
         }
       }
     }
@@ -891,10 +912,10 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       else
         continue;  // outside the tile: added per tile
       v = warp_sum(v);
-      if ((tid & 31) == 0) S.red[tid >> 5][RS_Z + j] += (double)v;
+      if ((tid & 31) == 0) red_slot_add<R>(S, tid >> 5, RS_Z + j, v);
     }
     const R tt = warp_sum(Tacc);
-    if ((tid & 31) == 0) S.red[tid >> 5][RS_T] += (double)tt;
+    if ((tid & 31) == 0) red_slot_add<R>(S, tid >> 5, RS_T, tt);
   }
   __syncthreads();
   // CTA totals -> partials[slot][blockIdx]
@@ -912,8 +933,8 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     if (slot >= 0) {
       double s = 0.0, tot = 0.0;
       for (int w = 0; w < NTHREADS / 32; ++w) {
-        s += S.red[w][tid];
-        tot += S.red[w][RS_T];
+        s += red_slot<R>(S, w, tid);
+        tot += red_slot<R>(S, w, RS_T);
       }
       // Z rotations: S_j = T - 2 U_j
       p.partials[(int64_t)slot * p.G + blockIdx.x] = tid >= RS_Z && tid < RS_T ? tot + sign * s : s;
