@@ -36,16 +36,10 @@ __device__ __forceinline__ double2 cmulb(double2 a, double2 b) {
 __device__ __forceinline__ float2 cmulb(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
-template <typename C>
-__device__ __forceinline__ C toc(double x, double y);
-template <>
-__device__ __forceinline__ double2 toc<double2>(double x, double y) {
-  return make_double2(x, y);
-}
-template <>
-__device__ __forceinline__ float2 toc<float2>(double x, double y) {
-  return make_float2((float)x, (float)y);
-}
+__device__ __forceinline__ float2 tocf(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ double2 tocf(double x, double y) { return make_double2(x, y); }
+__device__ __forceinline__ void sincosT(double a, double* s, double* c) { sincos(a, s, c); }
+__device__ __forceinline__ void sincosT(float a, float* s, float* c) { sincosf(a, s, c); }
 
 // XOR swizzle of the low index bits with the next ones: 8 (complex128) or 16
 // (complex64) amplitudes per 128-byte row, so tasks that stride over the low
@@ -64,9 +58,13 @@ __device__ __forceinline__ uint64_t lad_inv(uint64_t x, uint64_t odd, uint64_t e
   return x;
 }
 
-__device__ __forceinline__ double rform(double theta, int* form, double* kappa) {
-  double s, c;
-  sincos(0.5 * theta, &s, &c);
+// Scaled form of a rotation by theta, in the precision T of the job's
+// coefficients (double for complex128, float for complex64: a double
+// instruction holds the FP64 pipe for 16 cycles per warp).
+template <typename T>
+__device__ __forceinline__ T rform(T theta, int* form, T* kappa) {
+  T s, c;
+  sincosT((T)0.5 * theta, &s, &c);
   if (fabs(c) >= fabs(s)) {
     *form = 0;
     *kappa = c;
@@ -159,7 +157,7 @@ __device__ __forceinline__ R wsum(R v) {
 // 2^G amplitudes of one task (all other bits fixed) in registers.
 template <typename C, typename R, int G, int NT, bool DBL, int SG>
 __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, const int* axis, const int* form,
-                                          const double* u) {
+                                          const R* u) {
   const int ntask = M >> G;
   int b[G];
   int ax[G], fm[G];
@@ -205,7 +203,7 @@ __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, c
 // in out[0..G-1] (this warp's reduction slots).
 template <typename C, typename R, int G, int NT, bool DBL>
 __device__ __forceinline__ void red_group(const C* lam, const C* psi, int M, const int* bits, const int* axis,
-                                          double* out) {
+                                          R* out) {
   int b[G], ax[G];
   R acc[G];
 #pragma unroll
@@ -246,27 +244,30 @@ __device__ __forceinline__ void red_group(const C* lam, const C* psi, int M, con
 #pragma unroll
   for (int i = 0; i < G; ++i) {
     const R v = wsum(acc[i]);
-    if ((threadIdx.x & 31) == 0) out[i] = (double)v;
+    if ((threadIdx.x & 31) == 0) out[i] = v;
   }
 }
 
+// T: precision of the per-layer coefficients and partial sums (R)
+template <typename T>
 struct BShared {
   int job;
   int nxy, nz, ncross;       // gates of the current layer
   int xbit[BMAXQ];           // local bits of the X/Y rotations (cross rotation excluded)
   int xaxis[BMAXQ];
   int xslot[BMAXQ];          // output index
-  double xu[BMAXQ];
+  T xu[BMAXQ];
   int xform[BMAXQ];
   int caxis, cform, cslot;   // the cross rotation on the top bit (clusters)
-  double cu;
+  T cu;
   int zbit[BMAXQ];           // global bits of the Z rotations
   int zslot[BMAXQ];
-  double zs[BMAXQ], zc[BMAXQ];
-  double K;
-  double startP[BMAXQ + 1];
-  double tw[64];             // observable weights of the current job
-  double red[32][BMAXQ + 4];
+  T zs[BMAXQ], zc[BMAXQ];
+  T K;
+  int zpk[32];               // Z-table index bits of the element-loop step k (e = tid + NT k)
+  T startP[BMAXQ + 1];
+  T tw[64];                  // observable weights of the current job
+  T red[32][BMAXQ + 4];
 };
 
 }  // namespace
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
   using C = typename BatchC<R>::T;
   constexpr bool DBL = sizeof(R) == 8;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ BShared S;
+  __shared__ BShared<R> S;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int Mmax = 1 << mmax;
   // three state buffers: psi, lambda and a scratch that permutations and
@@ -325,15 +326,15 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       else
         leven |= b;
     }
-    if (tid == 0) {
+    if (tid <= n) {
+      // Ry(pi/4)^n |0>: amplitude cos(pi/8)^(n-k) sin(pi/8)^k, one k per thread
       double s8, c8;
       sincospi(0.125, &s8, &c8);
-      for (int k = 0; k <= n; ++k) {
-        double q = 1.0;
-        for (int i = 0; i < n - k; ++i) q *= c8;
-        for (int i = 0; i < k; ++i) q *= s8;
-        S.startP[k] = q;
-      }
+      const int k = tid;
+      double q = 1.0;
+      for (int i = 0; i < n - k; ++i) q *= c8;
+      for (int i = 0; i < k; ++i) q *= s8;
+      S.startP[k] = (R)q;
     }
     if (tid == 0 && rank == 0 && CS > 1) {
       if (J.expec) *J.expec = 0.0;
@@ -366,10 +367,10 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         const int q = lane;
         const bool valid = q < n;
         int axis = 0;
-        double th = 0.0;
+        R th = (R)0;
         if (valid) {
           axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
-          th = J.kind == 0 ? J.params[i * n + q] : J.params[2 * i];
+          th = (R)(J.kind == 0 ? J.params[i * n + q] : J.params[2 * i]);
         }
         const int b = n - 1 - q;
         const int slot = J.kind == 0 ? i * n + q : 2 * i;
@@ -377,9 +378,9 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         const bool iscross = valid && !isz && CS > 1 && b == m;
         const bool isxy = valid && !isz && !iscross;
         int f = 0;
-        double k = 1.0, u = 0.0, zs = 0.0, zc = 1.0;
-        if (isxy || iscross) u = rform(th, &f, &k);
-        if (isz) sincos(0.5 * th, &zs, &zc);
+        R k = (R)1, u = (R)0, zs = (R)0, zc = (R)1;
+        if (isxy || iscross) u = rform<R>(th, &f, &k);
+        if (isz) sincosT((R)0.5 * th, &zs, &zc);
         const unsigned mxy = __ballot_sync(full, isxy), mz = __ballot_sync(full, isz);
         const unsigned above = q == 31 ? 0u : (full << (q + 1));
         if (isxy) {
@@ -403,7 +404,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           S.cu = u;
           S.cform = f;
         }
-        double kk = (isxy || iscross) ? k : 1.0;
+        R kk = (isxy || iscross) ? k : (R)1;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) kk *= __shfl_xor_sync(full, kk, o);
         const unsigned mc = __ballot_sync(full, iscross);
@@ -420,14 +421,27 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     // The Z table is built by doubling: 2^nz complex multiplies in all.
     auto build_diag = [&](int i, bool inv) {
       const int nzt = S.nz < BZMAX ? S.nz : BZMAX;
-      if (J.kind == 0) {
-        if (tid == 0) ztab[0] = toc<C>(S.K, 0.0);
+      if (J.kind == 0 && !DBL) {
+        // complex64: every entry as its own product (nzt float multiplies),
+        // one barrier instead of one per Z rotation
+        for (int pp = tid; pp < (1 << nzt); pp += NT) {
+          C v = tocf(S.K, (R)0);
+          for (int j = 0; j < nzt; ++j) {
+            // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170); conjugated inverse
+            const bool one = (pp >> j) & 1;
+            const R sg = (one != inv) ? (R)1 : (R)-1;
+            v = cmulb(v, tocf(S.zc[j], sg * S.zs[j]));
+          }
+          ztab[pp] = v;
+        }
+      } else if (J.kind == 0) {
+        // complex128: doubling, 2^nzt complex multiplies in all
+        if (tid == 0) ztab[0] = tocf(S.K, (R)0);
         __syncthreads();
         for (int j = 0; j < nzt; ++j) {
           const int h = 1 << j;
-          // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170); conjugated inverse
-          const C e0 = toc<C>(S.zc[j], inv ? S.zs[j] : -S.zs[j]);
-          const C e1 = toc<C>(S.zc[j], inv ? -S.zs[j] : S.zs[j]);
+          const C e0 = tocf(S.zc[j], inv ? S.zs[j] : -S.zs[j]);
+          const C e1 = tocf(S.zc[j], inv ? -S.zs[j] : S.zs[j]);
           for (int pp = tid; pp < h; pp += NT) {
             const C v = ztab[pp];
             ztab[pp + h] = cmulb(v, e1);
@@ -436,13 +450,20 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           __syncthreads();
         }
       } else {
-        const double g = J.params[2 * i + 1] * J.cost_w0;
+        const R g = (R)(J.params[2 * i + 1] * J.cost_w0);
         const int MA = J.cost_maxabs;
         for (int k = tid; k <= 2 * MA; k += NT) {
-          double s, c;
-          sincos(g * (double)(k - MA), &s, &c);
-          ztab[k] = toc<C>(S.K * c, S.K * (inv ? s : -s));
+          R s, c;
+          sincosT(g * (R)(k - MA), &s, &c);
+          ztab[k] = tocf(S.K * c, S.K * (inv ? s : -s));
         }
+      }
+      // Z-table index bits of the element-loop steps (e = tid + NT k)
+      if (J.kind == 0 && tid < (M + NT - 1) / NT) {
+        int pat = 0;
+        const uint64_t xk = top | (uint64_t)(tid * NT);
+        for (int j = 0; j < nzt; ++j) pat |= (int)((xk >> S.zbit[j]) & 1) << j;
+        S.zpk[tid] = pat;
       }
       __syncthreads();
     };
@@ -459,17 +480,20 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     // per-element diagonal multiply on buffer v (table built by build_diag)
     auto apply_diag = [&](C* v, bool inv) {
       const int nzt = S.nz < BZMAX ? S.nz : BZMAX;
-      for (int e = tid; e < M; e += NT) {
+      // the pattern of e = tid + NT k is this thread's bits OR the step's
+      // (disjoint bit ranges; the top bit is in the step part)
+      int ptid = 0;
+      if (J.kind == 0)
+        for (int j = 0; j < nzt; ++j) ptid |= (int)(((uint64_t)tid >> S.zbit[j]) & 1) << j;
+      for (int e = tid, k = 0; e < M; e += NT, ++k) {
         const uint64_t x = top | (uint64_t)e;
         C a = v[swb(e, DBL)];
         if (J.kind == 0) {
-          int pat = 0;
-          for (int j = 0; j < nzt; ++j) pat |= (int)((x >> S.zbit[j]) & 1) << j;
-          a = cmulb(a, ztab[pat]);
+          a = cmulb(a, ztab[ptid | S.zpk[k]]);
           for (int j = BZMAX; j < S.nz; ++j) {
             const bool one = (x >> S.zbit[j]) & 1;
-            const double sgn = (one != inv) ? 1.0 : -1.0;
-            a = cmulb(a, toc<C>(S.zc[j], sgn * S.zs[j]));
+            const R sgn = (one != inv) ? (R)1 : (R)-1;
+            a = cmulb(a, tocf(S.zc[j], sgn * S.zs[j]));
           }
         } else {
           a = cmulb(a, ztab[cost_m(x) + J.cost_maxabs]);
@@ -557,16 +581,16 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     // adds onto 0, whose result does not depend on their order)
     auto emit1 = [&](R val, int slot, double factor) {
       const R v = wsum(val);
-      if (lane == 0) S.red[warp][0] = (double)v;
+      if (lane == 0) S.red[warp][0] = v;
       __syncthreads();
       if (tid == 0) {
-        double tot = 0.0;
+        R tot = (R)0;
         for (int w = 0; w < NT / 32; ++w) tot += S.red[w][0];
-        tot *= factor;
+        const double out = factor * (double)tot;
         if (CS > 1)
-          atomicAdd(&J.grad[slot], tot);
+          atomicAdd(&J.grad[slot], out);
         else
-          J.grad[slot] = tot;
+          J.grad[slot] = out;
       }
       __syncthreads();
     };
@@ -592,7 +616,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         const C v = psi[swb(e, DBL)];
         R lx = (R)0, ly = (R)0;
         if (costonly) {
-          const R d = (R)(J.cost_w0 * (double)cost_m(x));
+          const R d = (R)J.cost_w0 * (R)cost_m(x);
           lx = d * v.x;
           ly = d * v.y;
         } else {
@@ -634,15 +658,15 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         }
       }
       const R v = wsum(eacc);
-      if (lane == 0) S.red[warp][0] = (double)v;
+      if (lane == 0) S.red[warp][0] = v;
       __syncthreads();
       if (tid == 0) {
-        double tot = 0.0;
+        R tot = (R)0;
         for (int w = 0; w < NT / 32; ++w) tot += S.red[w][0];
         if (CS > 1)
-          atomicAdd(J.expec, tot);
+          atomicAdd(J.expec, (double)tot);
         else
-          *J.expec = tot;
+          *J.expec = (double)tot;
       }
       __syncthreads();
     }
@@ -681,7 +705,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
               a += rank == 0 ? -fma(l.x, qr.x, l.y * qr.y) : fma(l.x, qr.x, l.y * qr.y);
           }
           a = wsum(a);
-          if (lane == 0) S.red[warp][ns] = (double)a;
+          if (lane == 0) S.red[warp][ns] = a;
           ++ns;
         }
         // Z rotations: sum_x s_j(x) Im(conj lam psi) = T - 2 U_j.  With
@@ -710,31 +734,31 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
             else
               U = rank ? T : (R)0;
             R val = wsum(T - (R)2 * U);
-            if (lane == 0) S.red[warp][ns + j] = (double)val;
+            if (lane == 0) S.red[warp][ns + j] = val;
           }
           ns += nz;
         }
         __syncthreads();
         if (J.kind == 0) {
           if (tid < ns) {
-            double tot = 0.0;
+            R tot = (R)0;
             for (int w = 0; w < NT / 32; ++w) tot += S.red[w][tid];
             const int slot = tid < nxy ? S.xslot[tid] : (tid < nxy + ((CS > 1 && S.ncross) ? 1 : 0) ? S.cslot
                                                                                                     : S.zslot[tid - nxy - ((CS > 1 && S.ncross) ? 1 : 0)]);
             if (CS > 1)
-              atomicAdd(&J.grad[slot], tot);
+              atomicAdd(&J.grad[slot], (double)tot);
             else
-              J.grad[slot] = tot;
+              J.grad[slot] = (double)tot;
           }
         } else if (tid == 0) {
           // beta: the sum over all n X rotations of the layer
-          double tot = 0.0;
+          R tot = (R)0;
           for (int k = 0; k < ns; ++k)
             for (int w = 0; w < NT / 32; ++w) tot += S.red[w][k];
           if (CS > 1)
-            atomicAdd(&J.grad[2 * i], tot);
+            atomicAdd(&J.grad[2 * i], (double)tot);
           else
-            J.grad[2 * i] = tot;
+            J.grad[2 * i] = (double)tot;
         }
         __syncthreads();
         // the partner may still read this CTA's psi for its top-bit reduction
@@ -751,7 +775,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           for (int e = tid; e < M; e += NT) {
             const uint64_t x = top | (uint64_t)e;
             const C l = lam[swb(e, DBL)], q = psi[swb(e, DBL)];
-            gsum = fma((R)(J.cost_w0 * (double)cost_m(x)), fma(l.x, q.y, -l.y * q.x), gsum);
+            gsum = fma((R)J.cost_w0 * (R)cost_m(x), fma(l.x, q.y, -l.y * q.x), gsum);
           }
           emit1(gsum, 2 * i + 1, 2.0);
         }
