@@ -47,12 +47,13 @@ __device__ __forceinline__ void sincosT(float a, float* s, float* c) { sincosf(a
 __device__ __forceinline__ int swb(int e, bool dbl) { return dbl ? e ^ ((e >> 3) & 7) : e ^ ((e >> 4) & 15); }
 __device__ __forceinline__ int ins0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
 
-__device__ __forceinline__ uint64_t lad_fwd(uint64_t x, uint64_t odd, uint64_t even) {
+// index arithmetic of the batched kernel is 32-bit: its jobs have at most 26 qubits
+__device__ __forceinline__ uint32_t lad_fwd(uint32_t x, uint32_t odd, uint32_t even) {
   x ^= (x & odd) >> 1;
   x ^= (x & even) >> 1;
   return x;
 }
-__device__ __forceinline__ uint64_t lad_inv(uint64_t x, uint64_t odd, uint64_t even) {
+__device__ __forceinline__ uint32_t lad_inv(uint32_t x, uint32_t odd, uint32_t even) {
   x ^= (x & even) >> 1;
   x ^= (x & odd) >> 1;
   return x;
@@ -169,18 +170,24 @@ __device__ __forceinline__ void rot_group(C* v, C* v2, int M, const int* bits, c
     fm[i] = form[i];
     uu[i] = (R)u[i];
   }
+  // the swizzle is GF(2)-linear: a task's indices are its swizzled base
+  // XOR the swizzled group bits
+  int sbit[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) sbit[i] = swb(1 << b[i], DBL);
   for (int tk = threadIdx.x; tk < ntask; tk += NT) {
     int base = tk;
 #pragma unroll
     for (int i = 0; i < G; ++i) base = ins0(base, b[i]);
+    const int sb = swb(base, DBL);
     int idx[1 << G];
 #pragma unroll
     for (int c = 0; c < (1 << G); ++c) {
-      int x = base;
+      int x = sb;
 #pragma unroll
       for (int i = 0; i < G; ++i)
-        if ((c >> i) & 1) x |= 1 << b[i];
-      idx[c] = swb(x, DBL);
+        if ((c >> i) & 1) x ^= sbit[i];
+      idx[c] = x;
     }
 #pragma unroll
     for (int pass = 0; pass < 2; ++pass) {
@@ -213,19 +220,23 @@ __device__ __forceinline__ void red_group(const C* lam, const C* psi, int M, con
     acc[i] = (R)0;
   }
   const int ntask = M >> G;
+  int sbit[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) sbit[i] = swb(1 << b[i], DBL);
   for (int tk = threadIdx.x; tk < ntask; tk += NT) {
     int base = tk;
 #pragma unroll
     for (int i = 0; i < G; ++i) base = ins0(base, b[i]);
+    const int sb = swb(base, DBL);
     C la[1 << G], qa[1 << G];
 #pragma unroll
     for (int c = 0; c < (1 << G); ++c) {
-      int x = base;
+      int x = sb;
 #pragma unroll
       for (int i = 0; i < G; ++i)
-        if ((c >> i) & 1) x |= 1 << b[i];
-      la[c] = lam[swb(x, DBL)];
-      qa[c] = psi[swb(x, DBL)];
+        if ((c >> i) & 1) x ^= sbit[i];
+      la[c] = lam[x];
+      qa[c] = psi[x];
     }
 #pragma unroll
     for (int i = 0; i < G; ++i) {
@@ -315,12 +326,12 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     const int n = J.n;
     const int m = n - (CS > 1 ? 1 : 0);
     const int M = 1 << m;
-    const uint64_t top = (uint64_t)rank << m;
+    const uint32_t top = (uint32_t)rank << m;
     const bool grad = J.grad != nullptr;
     const int L = J.layers;
-    uint64_t lodd = 0, leven = 0;
+    uint32_t lodd = 0, leven = 0;
     for (int q = 0; q + 1 < n; ++q) {
-      const uint64_t b = 1ull << (n - 1 - q);
+      const uint32_t b = 1u << (n - 1 - q);
       if (q & 1)
         lodd |= b;
       else
@@ -348,9 +359,9 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     // start state
     const R plus = (R)exp2(-0.5 * n);
     for (int e = tid; e < M; e += NT) {
-      const uint64_t x = top | (uint64_t)e;
+      const uint32_t x = top | (uint32_t)e;
       C v;
-      v.x = J.kind == 0 ? (R)S.startP[__popcll(x)] : plus;
+      v.x = J.kind == 0 ? (R)S.startP[__popc(x)] : plus;
       v.y = (R)0;
       psi[swb(e, DBL)] = v;
     }
@@ -461,13 +472,13 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       // Z-table index bits of the element-loop steps (e = tid + NT k)
       if (J.kind == 0 && tid < (M + NT - 1) / NT) {
         int pat = 0;
-        const uint64_t xk = top | (uint64_t)(tid * NT);
+        const uint32_t xk = top | (uint32_t)(tid * NT);
         for (int j = 0; j < nzt; ++j) pat |= (int)((xk >> S.zbit[j]) & 1) << j;
         S.zpk[tid] = pat;
       }
       __syncthreads();
     };
-    auto cost_m = [&](uint64_t x) {
+    auto cost_m = [&](uint32_t x) {
       int mm = 0;
       for (int k = 0; k < J.cost_nterms; ++k) {
         const qg_cost_term t = J.cost[k];
@@ -484,9 +495,9 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       // (disjoint bit ranges; the top bit is in the step part)
       int ptid = 0;
       if (J.kind == 0)
-        for (int j = 0; j < nzt; ++j) ptid |= (int)(((uint64_t)tid >> S.zbit[j]) & 1) << j;
+        for (int j = 0; j < nzt; ++j) ptid |= (int)(((uint32_t)tid >> S.zbit[j]) & 1) << j;
       for (int e = tid, k = 0; e < M; e += NT, ++k) {
-        const uint64_t x = top | (uint64_t)e;
+        const uint32_t x = top | (uint32_t)e;
         C a = v[swb(e, DBL)];
         if (J.kind == 0) {
           a = cmulb(a, ztab[ptid | S.zpk[k]]);
@@ -507,8 +518,8 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     auto entangle = [&](C*& v, bool inv) {
       if (J.entangler == 2) {
         for (int e = tid; e < M; e += NT) {
-          const uint64_t x = top | (uint64_t)e;
-          if (__popcll(x & (x >> 1)) & 1) {
+          const uint32_t x = top | (uint32_t)e;
+          if (__popc(x & (x >> 1)) & 1) {
             C a = v[swb(e, DBL)];
             a.x = -a.x;
             a.y = -a.y;
@@ -519,9 +530,9 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         return;
       }
       for (int e = tid; e < M; e += NT) {
-        const uint64_t x = top | (uint64_t)e;
-        const uint64_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
-        scr[swb(e, DBL)] = v[swb((int)(src & (uint64_t)(M - 1)), DBL)];
+        const uint32_t x = top | (uint32_t)e;
+        const uint32_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
+        scr[swb(e, DBL)] = v[swb((int)(src & (uint32_t)(M - 1)), DBL)];
       }
       __syncthreads();
       C* t = v;
@@ -612,7 +623,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       R eacc = (R)0;
       const bool costonly = J.kind == 1 && grad;
       for (int e = tid; e < M; e += NT) {
-        const uint64_t x = top | (uint64_t)e;
+        const uint32_t x = top | (uint32_t)e;
         const C v = psi[swb(e, DBL)];
         R lx = (R)0, ly = (R)0;
         if (costonly) {
@@ -622,21 +633,21 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         } else {
           for (int k = 0; k < J.nterms; ++k) {
             const BatchTerm t = J.terms[k];
-            const uint64_t b0 = 1ull << (n - 1 - t.q0);
+            const uint32_t b0 = 1u << (n - 1 - t.q0);
             const R tw = k < BTERMS ? (R)S.tw[k] : (R)t.w;
             if (t.kind >= 2) {
               bool s = (x & b0) != 0;
-              if (t.kind == 3) s ^= (x & (1ull << (n - 1 - t.q1))) != 0;
+              if (t.kind == 3) s ^= (x & (1u << (n - 1 - t.q1))) != 0;
               const R w = s ? -tw : tw;
               lx = fma(w, v.x, lx);
               ly = fma(w, v.y, ly);
             } else {
-              const uint64_t xp = x ^ b0;
+              const uint32_t xp = x ^ b0;
               C u;
               if ((xp >> m) != (x >> m))
-                u = remote(psi)[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
+                u = remote(psi)[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
               else
-                u = psi[swb((int)(xp & (uint64_t)(M - 1)), DBL)];
+                u = psi[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
               const R w = tw;
               if (t.kind == 0) {
                 lx = fma(w, u.x, lx);
@@ -773,7 +784,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           // lambda and psi carry no scale factor
           R gsum = (R)0;
           for (int e = tid; e < M; e += NT) {
-            const uint64_t x = top | (uint64_t)e;
+            const uint32_t x = top | (uint32_t)e;
             const C l = lam[swb(e, DBL)], q = psi[swb(e, DBL)];
             gsum = fma((R)J.cost_w0 * (R)cost_m(x), fma(l.x, q.y, -l.y * q.x), gsum);
           }
