@@ -276,6 +276,7 @@ struct BShared {
   T zs[BMAXQ], zc[BMAXQ];
   T K;
   int zpk[32];               // Z-table index bits of the element-loop step k (e = tid + NT k)
+  int zpkf[32];              // the same for the ladder image lad_fwd(top | NT k) (backward fusion)
   T startP[BMAXQ + 1];
   T tw[64];                  // observable weights of the current job
   T red[32][BMAXQ + 4];
@@ -471,10 +472,15 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       }
       // Z-table index bits of the element-loop steps (e = tid + NT k)
       if (J.kind == 0 && tid < (M + NT - 1) / NT) {
-        int pat = 0;
+        int pat = 0, patf = 0;
         const uint32_t xk = top | (uint32_t)(tid * NT);
-        for (int j = 0; j < nzt; ++j) pat |= (int)((xk >> S.zbit[j]) & 1) << j;
+        const uint32_t xf = lad_fwd(xk, lodd, leven);
+        for (int j = 0; j < nzt; ++j) {
+          pat |= (int)((xk >> S.zbit[j]) & 1) << j;
+          patf |= (int)((xf >> S.zbit[j]) & 1) << j;
+        }
         S.zpk[tid] = pat;
+        S.zpkf[tid] = patf;
       }
       __syncthreads();
     };
@@ -606,12 +612,54 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       __syncthreads();
     };
 
+    // McClean layers with the entangler before the rotations: the ladder
+    // and the layer's diagonal in one pass.  Forward v <- D (E v):
+    // new[x] = D[x] v[A^{-1} x]; backward v <- E^{-1} (D^{-1} v):
+    // new[x] = D^{-1}[A x] v[A x].  The table index of A x is linear in x,
+    // so it splits into a per-thread and a per-step part like the plain one.
+    const bool fuse = J.kind == 0 && J.entangler != 0 && J.placement == 0;
+    auto entangle_diag = [&](C*& v, bool inv) {
+      const int nzt = S.nz;  // callers fuse only when every Z rotation is in the table
+      int ptid = 0;
+      const uint32_t tsrc = (inv && J.entangler == 1) ? lad_fwd((uint32_t)tid, lodd, leven) : (uint32_t)tid;
+      for (int j = 0; j < nzt; ++j) ptid |= (int)((tsrc >> S.zbit[j]) & 1) << j;
+      if (J.entangler == 2) {
+        // CZ: a sign, its own inverse, in place
+        for (int e = tid, k = 0; e < M; e += NT, ++k) {
+          const uint32_t x = top | (uint32_t)e;
+          C a = cmulb(v[swb(e, DBL)], ztab[ptid | S.zpk[k]]);
+          if (__popc(x & (x >> 1)) & 1) {
+            a.x = -a.x;
+            a.y = -a.y;
+          }
+          v[swb(e, DBL)] = a;
+        }
+        __syncthreads();
+        return;
+      }
+      for (int e = tid, k = 0; e < M; e += NT, ++k) {
+        const uint32_t x = top | (uint32_t)e;
+        const uint32_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
+        const int pat = inv ? (ptid ^ S.zpkf[k]) : (ptid | S.zpk[k]);
+        scr[swb(e, DBL)] = cmulb(v[swb((int)(src & (uint32_t)(M - 1)), DBL)], ztab[pat]);
+      }
+      __syncthreads();
+      C* t = v;
+      v = scr;
+      scr = t;
+    };
+
     // ---- forward
     for (int i = 0; i < L; ++i) {
       setup_layer(i);
-      if (J.kind == 0 && J.entangler != 0 && J.placement == 0) entangle(psi, false);
-      build_diag(i, false);
-      apply_diag(psi, false);
+      if (fuse && S.nz <= BZMAX) {
+        build_diag(i, false);
+        entangle_diag(psi, false);
+      } else {
+        if (fuse) entangle(psi, false);
+        build_diag(i, false);
+        apply_diag(psi, false);
+      }
       if (CS > 1) cluster.sync();
       rotate(psi, nullptr, false);
       if (J.kind == 0 && J.entangler != 0 && J.placement == 1) entangle(psi, false);
@@ -777,6 +825,12 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         // inverse rotations on lam and psi
         psi = rotate(lam, psi, true);
         build_diag(i, true);
+        if (fuse && S.nz <= BZMAX) {
+          entangle_diag(lam, true);
+          entangle_diag(psi, true);
+          if (CS > 1) cluster.sync();
+          continue;
+        }
         apply_diag(lam, true);
         apply_diag(psi, true);
         if (J.kind == 1) {
