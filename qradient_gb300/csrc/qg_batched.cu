@@ -259,6 +259,86 @@ __device__ __forceinline__ void red_group(const C* lam, const C* psi, int M, con
   }
 }
 
+// Backward: the gradient reductions of G rotations and their inverses on
+// lambda and psi in one pass.  The rotations of a layer commute with each
+// other's Paulis and with their own, so Im<lam|P|psi> is the same before and
+// after any of them is applied to both states; a group's sums are taken
+// from the loaded amplitudes, then both states are rotated back and stored.
+// The scaled forms divide each state by the rotation's kappa, so sums taken
+// after earlier groups carry 1 / prod(kappa^2) of those groups: `scale`
+// (that product) restores them.
+template <typename C, typename R, int G, int NT, bool DBL>
+__device__ __forceinline__ void rotred_group(C* lam, C* psi, int M, const int* bits, const int* axis, const int* form,
+                                             const R* u, R scale, R* out) {
+  int b[G], ax[G], fm[G];
+  R uu[G], acc[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    b[i] = bits[i];
+    ax[i] = axis[i];
+    fm[i] = form[i];
+    uu[i] = u[i];
+    acc[i] = (R)0;
+  }
+  int sbit[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) sbit[i] = swb(1 << b[i], DBL);
+  const int ntask = M >> G;
+  for (int tk = threadIdx.x; tk < ntask; tk += NT) {
+    int base = tk;
+#pragma unroll
+    for (int i = 0; i < G; ++i) base = ins0(base, b[i]);
+    const int sb = swb(base, DBL);
+    int idx[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      int x = sb;
+#pragma unroll
+      for (int i = 0; i < G; ++i)
+        if ((c >> i) & 1) x ^= sbit[i];
+      idx[c] = x;
+    }
+    C la[1 << G], qa[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      la[c] = lam[idx[c]];
+      qa[c] = psi[idx[c]];
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      if (ax[i] == 0) {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] += redp<C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], 0);
+      } else {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] += redp<C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], 1);
+      }
+    }
+    rotb_any<-1, 0, G>(la, ax[0], fm[0], uu[0]);
+    rotb_any<-1, 0, G>(qa, ax[0], fm[0], uu[0]);
+    if (G > 1) {
+      rotb_any<-1, (G > 1 ? 1 : 0), G>(la, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
+      rotb_any<-1, (G > 1 ? 1 : 0), G>(qa, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
+    }
+    if (G > 2) {
+      rotb_any<-1, (G > 2 ? 2 : 0), G>(la, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
+      rotb_any<-1, (G > 2 ? 2 : 0), G>(qa, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
+    }
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      lam[idx[c]] = la[c];
+      psi[idx[c]] = qa[c];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    const R v = wsum(acc[i]);
+    if ((threadIdx.x & 31) == 0) out[i] = v * scale;
+  }
+}
+
 // T: precision of the per-layer coefficients and partial sums (R)
 template <typename T>
 struct BShared {
@@ -268,6 +348,7 @@ struct BShared {
   int xaxis[BMAXQ];
   int xslot[BMAXQ];          // output index
   T xu[BMAXQ];
+  T xk[BMAXQ];               // scale factor kappa of each X/Y rotation (scaled form = rotation / kappa)
   int xform[BMAXQ];
   int caxis, cform, cslot;   // the cross rotation on the top bit (clusters)
   T cu;
@@ -401,6 +482,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           S.xaxis[idx] = axis;
           S.xslot[idx] = slot;
           S.xu[idx] = u;
+          S.xk[idx] = k;
           S.xform[idx] = f;
         }
         if (isz) {
@@ -546,6 +628,32 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       scr = t;
     };
     // X/Y rotations of the layer in groups of up to 3 bits per shared-memory pass
+    // rotation on the top bit (2-CTA clusters): the partner amplitude lives
+    // in the other CTA; new values go to the scratch buffer, which then
+    // becomes the rotated buffer
+    auto rotate_cross = [&](C*& v, C*& v2, bool inverse) {
+      if (CS > 1 && S.ncross) {
+        for (int pass = 0; pass < (v2 ? 2 : 1); ++pass) {
+          C*& w = pass ? v2 : v;
+          cluster.sync();
+          const C* rw = remote(w);
+          for (int e = tid; e < M; e += NT) {
+            const C own = w[swb(e, DBL)];
+            const C rem = rw[swb(e, DBL)];
+            C x0 = rank == 0 ? own : rem, x1 = rank == 0 ? rem : own;
+            if (inverse)
+              rotp<-1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
+            else
+              rotp<1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
+            scr[swb(e, DBL)] = rank == 0 ? x0 : x1;
+          }
+          cluster.sync();
+          C* t = w;
+          w = scr;
+          scr = t;
+        }
+      }
+    };
     auto rotate = [&](C*& v, C* v2in, bool inverse) {
       C* v2 = v2in;
       const int nxy = S.nxy;
@@ -568,29 +676,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         }
         __syncthreads();
       }
-      if (CS > 1 && S.ncross) {
-        // rotation on the top bit: the partner amplitude lives in the other
-        // CTA; new values go to the scratch buffer, which then becomes v
-        for (int pass = 0; pass < (v2 ? 2 : 1); ++pass) {
-          C*& w = pass ? v2 : v;
-          cluster.sync();
-          const C* rw = remote(w);
-          for (int e = tid; e < M; e += NT) {
-            const C own = w[swb(e, DBL)];
-            const C rem = rw[swb(e, DBL)];
-            C x0 = rank == 0 ? own : rem, x1 = rank == 0 ? rem : own;
-            if (inverse)
-              rotp<-1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
-            else
-              rotp<1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
-            scr[swb(e, DBL)] = rank == 0 ? x0 : x1;
-          }
-          cluster.sync();
-          C* t = w;
-          w = scr;
-          scr = t;
-        }
-      }
+      rotate_cross(v, v2, inverse);
       return v2;
     };
 
@@ -740,19 +826,42 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           entangle(lam, true);
           if (CS > 1) cluster.sync();
         }
-        // reductions at the end point of the layer's rotations; per-warp sums in S.red[warp][k]
+        // gradient reductions of the X/Y rotations on local bits fused with
+        // their inverses on lam and psi; per-warp sums in S.red[warp][k].
+        // The remaining sums (top bit, Z) are invariant under these
+        // rotations and are taken afterwards.
         const int nxy = S.nxy;
-        for (int g0 = 0; g0 < nxy; g0 += 3) {
+        R sc = (R)1;  // prod kappa^2 of the rotations already applied
+        if (DBL) {
+          // complex128: separate reduction passes at the layer's end point;
+          // the fused form needs more than the 128 registers a thread has here
+          for (int g0 = 0; g0 < nxy; g0 += 3) {
+            const int g = nxy - g0 < 3 ? nxy - g0 : 3;
+            if (g == 3)
+              red_group<C, R, 3, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+            else if (g == 2)
+              red_group<C, R, 2, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+            else
+              red_group<C, R, 1, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+          }
+        }
+        for (int g0 = 0; !DBL && g0 < nxy; g0 += 3) {
           const int g = nxy - g0 < 3 ? nxy - g0 : 3;
           if (g == 3)
-            red_group<C, R, 3, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+            rotred_group<C, R, 3, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sc,
+                                           &S.red[warp][g0]);
           else if (g == 2)
-            red_group<C, R, 2, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+            rotred_group<C, R, 2, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sc,
+                                           &S.red[warp][g0]);
           else
-            red_group<C, R, 1, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, &S.red[warp][g0]);
+            rotred_group<C, R, 1, NT, DBL>(lam, psi, M, S.xbit + g0, S.xaxis + g0, S.xform + g0, S.xu + g0, sc,
+                                           &S.red[warp][g0]);
+          for (int i = g0; i < g0 + g; ++i) sc *= S.xk[i] * S.xk[i];
+          __syncthreads();
         }
         int ns = nxy;
         if (CS > 1 && S.ncross) {
+          cluster.sync();  // the partner's psi has its local rotations applied
           R a = (R)0;
           for (int e = tid; e < M; e += NT) {
             const C l = lam[swb(e, DBL)];
@@ -764,7 +873,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
               a += rank == 0 ? -fma(l.x, qr.x, l.y * qr.y) : fma(l.x, qr.x, l.y * qr.y);
           }
           a = wsum(a);
-          if (lane == 0) S.red[warp][ns] = a;
+          if (lane == 0) S.red[warp][ns] = a * sc;
           ++ns;
         }
         // Z rotations: sum_x s_j(x) Im(conj lam psi) = T - 2 U_j.  With
@@ -793,7 +902,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
             else
               U = rank ? T : (R)0;
             R val = wsum(T - (R)2 * U);
-            if (lane == 0) S.red[warp][ns + j] = val;
+            if (lane == 0) S.red[warp][ns + j] = val * sc;
           }
           ns += nz;
         }
@@ -823,7 +932,10 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         // the partner may still read this CTA's psi for its top-bit reduction
         if (CS > 1) cluster.sync();
         // inverse rotations on lam and psi
-        psi = rotate(lam, psi, true);
+        if (DBL)
+          psi = rotate(lam, psi, true);
+        else
+          rotate_cross(lam, psi, true);
         build_diag(i, true);
         if (fuse && S.nz <= BZMAX) {
           entangle_diag(lam, true);
