@@ -450,8 +450,21 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     __syncthreads();
 
     // ---- helpers bound to this job
-    // layer setup: rotations of layer i into S (forward coefficients)
-    auto setup_layer = [&](int i) {
+    // warp 0 keeps the next layer's angle and axis in registers: the loads
+    // are issued one layer ahead, so a layer setup does not wait on memory
+    // while the other warps wait at its barrier
+    int pf_layer = -1, pf_axis = 0;
+    double pf_th = 0.0;
+    auto prefetch = [&](int i) {
+      pf_layer = i;
+      if (i >= 0 && i < L && lane < n) {
+        pf_axis = J.kind == 0 ? (int)J.axes[i * n + lane] : 0;
+        pf_th = J.kind == 0 ? J.params[i * n + lane] : J.params[2 * i];
+      }
+    };
+    // layer setup: rotations of layer i into S (forward coefficients); the
+    // next layer to be set up is i + step
+    auto setup_layer = [&](int i, int step) {
       // warp 0, lane q = qubit q: coefficients in parallel; the X/Y and Z
       // lists are compacted in ascending bit order (descending q) with
       // ballots, and K is a shuffle product over the warp
@@ -459,12 +472,10 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         const unsigned full = 0xffffffffu;
         const int q = lane;
         const bool valid = q < n;
-        int axis = 0;
-        R th = (R)0;
-        if (valid) {
-          axis = J.kind == 0 ? (int)J.axes[i * n + q] : 0;
-          th = (R)(J.kind == 0 ? J.params[i * n + q] : J.params[2 * i]);
-        }
+        if (pf_layer != i) prefetch(i);
+        const int axis = valid ? pf_axis : 0;
+        const R th = valid ? (R)pf_th : (R)0;
+        prefetch(i + step);
         const int b = n - 1 - q;
         const int slot = J.kind == 0 ? i * n + q : 2 * i;
         const bool isz = valid && axis == 2;
@@ -737,7 +748,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
 
     // ---- forward
     for (int i = 0; i < L; ++i) {
-      setup_layer(i);
+      setup_layer(i, 1);
       if (fuse && S.nz <= BZMAX) {
         build_diag(i, false);
         entangle_diag(psi, false);
@@ -820,7 +831,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     // ---- backward (uncompute form)
     if (grad) {
       for (int i = L - 1; i >= 0; --i) {
-        setup_layer(i);
+        setup_layer(i, -1);
         if (J.kind == 0 && J.entangler != 0 && J.placement == 1) {
           entangle(psi, true);
           entangle(lam, true);
