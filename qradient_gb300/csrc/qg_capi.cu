@@ -583,6 +583,7 @@ std::vector<ObsDesc> build_obs(const qg_circuit* c, const Program& P, bool grad,
         o.b0 = (int8_t)(n - 1 - tm.q0);
         o.b1 = (int8_t)(tm.kind == QG_PAULI_ZZ ? n - 1 - tm.q1 : 0);
         o.w = tm.w;
+        o.wf = (float)tm.w;
       }
       d->ndiag = k;
       // weight runs (the terms are sorted by weight): the kernel sums the
@@ -600,6 +601,7 @@ std::vector<ObsDesc> build_obs(const qg_circuit* c, const Program& P, bool grad,
       o.b0 = (int8_t)b;
       o.lb0 = (int8_t)local_of(lay.tiles[s], b);
       o.w = tm.w;
+        o.wf = (float)tm.w;
       ++nxy;
     }
     d->nxy = nxy;

@@ -112,6 +112,7 @@ struct ObsTerm {
   int8_t lb0;     // local tile bit of b0 (X/Y terms)
   int8_t endgrp;  // diagonal terms: the last of a run of equal weights
   int8_t pad[3];
+  float wf;       // w in single precision (complex64 observable)
   double w;
 };
 

@@ -268,6 +268,7 @@ struct SetupShared {
     float redf[NTHREADS / 32][RS_N];
   };
   float uf[TMAX];
+  float zsf[ZMAX], zcf[ZMAX];  // float copies of the Z phases (complex64 table)
 };
 
 // this warp's partial-sum slot in the kernel's own precision
@@ -296,6 +297,7 @@ __device__ __forceinline__ int64_t deposit(int64_t v, const uint8_t* bits, int n
 // table, both stored in the state's precision.
 template <typename C, bool BWD>
 __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShared& S, C* ztab, C* ctab) {
+  using R = decltype(C{}.x);
   const int tid = threadIdx.x;
   const int t = d.t, n = d.n;
   if (tid < d.nxy) {
@@ -364,7 +366,11 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
       rot_form(angle_of(d.scale[i], params), &f, &k);
       S.sc[i] = k;
     }
-    if (tid < d.nz) sincos(0.5 * angle_of(d.z[tid].a, params), &S.zs[tid], &S.zc[tid]);
+    if (tid < d.nz) {
+      sincos(0.5 * angle_of(d.z[tid].a, params), &S.zs[tid], &S.zc[tid]);
+      S.zsf[tid] = (float)S.zs[tid];
+      S.zcf[tid] = (float)S.zc[tid];
+    }
   }
   __syncthreads();
   if (d.has_diag && tid == 0) {
@@ -376,13 +382,39 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
   const double K = d.has_diag ? S.K : 1.0;
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   if (d.has_diag && !fold) {
+    // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170),
+    // times the layer scale K; conjugated for the backward sweep
     const int nz = d.nz;
-    for (int pat = tid; pat < (1 << nz); pat += NTHREADS) {
-      double2 ph = make_double2(K, 0.0);
-      // exp(-i theta/2) on bit 0, exp(+i theta/2) on bit 1 (state.py:168-170)
-      for (int j = 0; j < nz; ++j) ph = cmul(ph, make_double2(S.zc[j], ((pat >> j) & 1) ? S.zs[j] : -S.zs[j]));
-      if (BWD) ph.y = -ph.y;
-      ztab[pat] = to_c<C>(ph);
+    if (sizeof(R) == 8) {
+      // complex128: doubling, 2^nz complex multiplies in all (a product per
+      // entry would cost nz times that on the FP64 pipe, in every CTA)
+      if (tid == 0) ztab[0] = to_c<C>(make_double2(K, 0.0));
+      __syncthreads();
+      for (int j = 0; j < nz; ++j) {
+        const int h = 1 << j;
+        const double zs = BWD ? -S.zs[j] : S.zs[j];
+        const C e0 = to_c<C>(make_double2(S.zc[j], -zs)), e1 = to_c<C>(make_double2(S.zc[j], zs));
+        for (int pp = tid; pp < h; pp += NTHREADS) {
+          const C v = ztab[pp];
+          ztab[pp + h] = cmul(v, e1);
+          ztab[pp] = cmul(v, e0);
+        }
+        __syncthreads();
+      }
+    } else {
+      // complex64: a float product per entry, no barriers
+      const float Kf = (float)K;
+      for (int pat = tid; pat < (1 << nz); pat += NTHREADS) {
+        float2 ph = make_float2(Kf, 0.f);
+        for (int j = 0; j < nz; ++j) {
+          const float zs = ((pat >> j) & 1) ? S.zsf[j] : -S.zsf[j];
+          ph = cmul(ph, make_float2(S.zcf[j], BWD ? -zs : zs));
+        }
+        C v;
+        v.x = (R)ph.x;
+        v.y = (R)ph.y;
+        ztab[pat] = v;
+      }
     }
   }
   if (d.cost == COST_INT) {
@@ -982,6 +1014,7 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
   const int64_t ntiles = (int64_t)1 << (n - t);
   const LadderMasks lm = ladder_masks(n);
   double eacc = 0.0;
+  const R w0r = (R)d.cost_w0;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, outside, n - t);
     if (active) {
@@ -1000,17 +1033,21 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
     }
     if (d.nxy > 0) __syncthreads();  // X/Y terms read partners other threads loaded
     if (active) {
+      R tacc = (R)0;
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
         const C v = tile[sw<R>(e)];
-        double lx = 0.0, ly = 0.0;
+        // per-amplitude arithmetic in the state's precision (a double
+        // instruction in the complex64 kernel costs 16 cycles of the FP64
+        // pipe per warp); the expectation is accumulated in double per tile
+        R lx = (R)0, ly = (R)0;
         if (d.cost == COST_INT || d.cost == COST_REAL || d.ndiag > 0) {
-          double dv = 0.0;
+          R dv = (R)0;
           if (d.cost == COST_INT) {
-            dv = d.cost_w0 * (double)cost_i[x];
+            dv = w0r * (R)cost_i[x];
           } else if (d.cost == COST_REAL) {
-            dv = cost_d[x];
+            dv = (R)cost_d[x];
           } else {
             // integer sign sums per run of equal weights, one multiply per
             // run: the inner loop is integer only, so the compiler cannot
@@ -1019,47 +1056,49 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
             while (i < d.ndiag) {
               int cnt = 0;
               bool last;
-              double w;
+              R w;
               do {
                 const ObsTerm& tm = d.term[i++];
                 const uint64_t m = (1ull << tm.b0) | (tm.kind == 3 ? (1ull << tm.b1) : 0ull);
                 cnt += 1 - 2 * (__popcll(x & m) & 1);
                 last = tm.endgrp;
-                w = tm.w;
+                w = sizeof(R) == 4 ? (R)tm.wf : (R)tm.w;
               } while (!last && i < d.ndiag);
-              dv = fma(w, (double)cnt, dv);
+              dv = fma(w, (R)cnt, dv);
             }
           }
-          lx = dv * (double)v.x;
-          ly = dv * (double)v.y;
+          lx = dv * v.x;
+          ly = dv * v.y;
         }
         for (int i = d.ndiag; i < d.ndiag + d.nxy; ++i) {
           const ObsTerm& tm = d.term[i];
           const C u = tile[sw<R>(e ^ (1 << tm.lb0))];
+          const R w = sizeof(R) == 4 ? (R)tm.wf : (R)tm.w;
           if (tm.kind == 0) {
-            lx = fma(tm.w, (double)u.x, lx);
-            ly = fma(tm.w, (double)u.y, ly);
+            lx = fma(w, u.x, lx);
+            ly = fma(w, u.y, ly);
           } else {
             // (Y psi)_x = -i psi_partner (bit 0) or +i psi_partner (bit 1)
-            const double sgn = ((x >> tm.b0) & 1) ? 1.0 : -1.0;
-            lx = fma(-sgn * tm.w, (double)u.y, lx);
-            ly = fma(sgn * tm.w, (double)u.x, ly);
+            const R sw_ = ((x >> tm.b0) & 1) ? w : -w;
+            lx = fma(-sw_, u.y, lx);
+            ly = fma(sw_, u.x, ly);
           }
         }
-        eacc = fma((double)v.x, lx, fma((double)v.y, ly, eacc));
+        tacc = fma(v.x, lx, fma(v.y, ly, tacc));
         if (d.store) {
           C o;
           if (d.accumulate) {
             o = lam[x];
-            o.x = (R)((double)o.x + lx);
-            o.y = (R)((double)o.y + ly);
+            o.x = o.x + lx;
+            o.y = o.y + ly;
           } else {
-            o.x = (R)lx;
-            o.y = (R)ly;
+            o.x = lx;
+            o.y = ly;
           }
           lam[x] = o;
         }
       }
+      eacc += (double)tacc;
     }
     if (d.nxy > 0) __syncthreads();
   }
