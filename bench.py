@@ -554,10 +554,13 @@ def main():
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     traffic = None
+    pipe_busy = None
     tpath = os.path.join(ROOT, "profiles", "backward_sweep_traffic.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get("dram_bytes_per_launch")
+            prof = json.load(open(tpath))
+            traffic = prof.get("dram_bytes_per_launch")
+            pipe_busy = prof.get("fp64_pipe_busy_ncu")
         except ValueError:
             traffic = None
     if args.dtype == "complex128":
@@ -565,6 +568,10 @@ def main():
                 "peak": fp64_peak_tflops, "unit": "TFLOP/s",
                 "frac": achieved_tflops / fp64_peak_tflops if achieved_tflops else None, "traffic": traffic,
                 "peak_source": "measured live: FP64 FMA chain probe (qg_probe_fp64_fma_rate) x 2",
+                "note": "achieved counts the reference's 6 flops per rotation and 4 per gradient reduction per "
+                        "amplitude; the kernels' scaled rotation forms execute 4 per rotation, so the fraction reads "
+                        "above 1; the FP64 pipe itself is fp64_pipe_busy_ncu of its peak (ncu, per launch)",
+                "fp64_pipe_busy_ncu": pipe_busy,
                 "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                         "frac": achieved_gbs / hbm_peak if achieved_gbs else None,
                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
