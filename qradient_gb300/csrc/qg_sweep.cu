@@ -295,8 +295,12 @@ __device__ __forceinline__ int64_t deposit(int64_t v, const uint8_t* bits, int n
 // Common per-CTA setup: gate coefficients, element offsets, outside bits,
 // the diagonal phase table (Z rotations * scale) and the integer-cost phase
 // table, both stored in the state's precision.
+// ladk (complex64 kernels; null for complex128): the CNOT-ladder image of
+// offhi[k] (A^-1 forward, A backward), so an element's image is the XOR of
+// its parts' images
 template <typename C, bool BWD>
-__device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShared& S, C* ztab, C* ctab) {
+__device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShared& S, C* ztab, C* ctab,
+                            int64_t* ladk = nullptr) {
   using R = decltype(C{}.x);
   const int tid = threadIdx.x;
   const int t = d.t, n = d.n;
@@ -329,13 +333,16 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
   }
   for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;  // clears both views
   if (t > 8) {
+    const LadderMasks lm = ladder_masks(n);
     for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) {
       S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
       S.zpk[k] = zpattern((uint64_t)S.offhi[k], d);
+      if (ladk) ladk[k] = (int64_t)(BWD ? ladder_fwd((uint64_t)S.offhi[k], lm) : ladder_inv((uint64_t)S.offhi[k], lm));
     }
   } else if (tid == 0) {
     S.offhi[0] = 0;
     S.zpk[0] = 0;
+    if (ladk) ladk[0] = 0;
   }
   if (tid == 0) {
     // bits not in the tile, ascending
@@ -639,7 +646,8 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   C* tile = (C*)smem;
   C* ztab = tile + tsize;
   C* ctab = ztab + (1 << d.nz);
-  sweep_setup<C, false>(d, p.params, S, ztab, ctab);
+  __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
+  sweep_setup<C, false>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -647,6 +655,9 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int zpt = zpattern((uint64_t)dep_lo, d);
+  // the ladder map is GF(2)-linear: the image of base | dep_lo | offhi[k]
+  // is the XOR of the three parts' images
+  const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);
   const int64_t ntiles = (int64_t)1 << (n - t);
   const R plus = (R)exp2(-0.5 * n);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
@@ -655,11 +666,16 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
     const int zp = zpt | zpattern((uint64_t)base, d);
+    const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
     if (active) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        const uint64_t src = d.pre == ENT_CNOT ? ladder_inv(x, lm) : x;
+        // complex64 takes the ladder image from its parts; complex128, bound
+        // by the FP64 pipe, computes it (integer work there is free, a
+        // shared-memory load is not)
+        const uint64_t src =
+            d.pre == ENT_CNOT ? (sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_inv(x, lm)) : x;
         C v;
         if (d.start == START_LOAD) {
           v = p.psi_in[src];
@@ -722,7 +738,8 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
   C* buf0 = (C*)smem;
   C* ztab = buf0 + 2 * tsize;
   C* ctab = ztab + (1 << d.nz);
-  sweep_setup<C, false>(d, p.params, S, ztab, ctab);
+  __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
+  sweep_setup<C, false>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -735,13 +752,16 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
 
   // copies of one tile into dst: this thread's elements only
+  const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts'
   auto issue = [&](int64_t tileid, C* dst) {
     if (active) {
       const int64_t base = deposit(tileid, S.outside, n - t);
+      const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        const uint64_t src = d.pre == ENT_CNOT ? ladder_inv(x, lm) : x;
+        const uint64_t src =
+            d.pre == ENT_CNOT ? (sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_inv(x, lm)) : x;
         cp_async_elem(&dst[sw<R>(e)], p.psi_in + src);
       }
     }
@@ -810,7 +830,8 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   C* tp = tl + tsize;
   C* ztab = tp + tsize;
   C* ctab = ztab + (1 << d.nz);
-  sweep_setup<C, true>(d, p.params, S, ztab, ctab);
+  __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
+  sweep_setup<C, true>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -818,6 +839,7 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int zpt = zpattern((uint64_t)dep_lo, d);
+  const uint64_t ldep = ladder_fwd((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts
   const int64_t ntiles = (int64_t)1 << (n - t);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
@@ -847,6 +869,7 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = deposit(tileid, S.outside, n - t);
     const int zp = zpt | zpattern((uint64_t)base, d);
+    const uint64_t lbase = ladder_fwd((uint64_t)base, lm) ^ ldep;
     R tT = (R)0, tG = (R)0;
     if (active) {
       // all of this thread's loads of the tile in flight at once (asynchronous
@@ -856,8 +879,14 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
         // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y]
-        cp_async_elem(&tl[sw<R>(e)], p.lam_in + (d.lam_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
-        cp_async_elem(&tp[sw<R>(e)], p.psi_in + (d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
+        if (sizeof(R) == 4) {
+          const uint64_t ax = lbase ^ (uint64_t)ladk[k];
+          cp_async_elem(&tl[sw<R>(e)], p.lam_in + (d.lam_undo == ENT_CNOT ? ax : x));
+          cp_async_elem(&tp[sw<R>(e)], p.psi_in + (d.psi_undo == ENT_CNOT ? ax : x));
+        } else {
+          cp_async_elem(&tl[sw<R>(e)], p.lam_in + (d.lam_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
+          cp_async_elem(&tp[sw<R>(e)], p.psi_in + (d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
+        }
       }
       cp_async_commit();
       cp_async_wait<0>();
