@@ -512,19 +512,39 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
     fm[i] = S.form[g0 + i];
     uu[i] = sizeof(R) == 4 ? (R)S.uf[g0 + i] : (R)S.u[g0 + i];
   }
+  // complex64: the swizzle is GF(2)-linear, so a task's indices are its
+  // swizzled base XOR the swizzled group bits (fewer integer instructions;
+  // complex128, bound by the FP64 pipe, keeps the direct form)
+  int sbit[sizeof(R) == 4 ? G : 1];
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int i = 0; i < G; ++i) sbit[i] = sw<R>(1 << b[i]);
+  }
   const int ntask = tsize >> G;
   for (int tk = threadIdx.x; tk < ntask; tk += NTHREADS) {
     int base = tk;
 #pragma unroll
     for (int i = 0; i < G; ++i) base = insert0(base, b[i]);
     int idx[1 << G];
+    if constexpr (sizeof(R) == 4) {
+      const int sb = sw<R>(base);
 #pragma unroll
-    for (int c = 0; c < (1 << G); ++c) {
-      int x = base;
+      for (int c = 0; c < (1 << G); ++c) {
+        int x = sb;
 #pragma unroll
-      for (int i = 0; i < G; ++i)
-        if ((c >> i) & 1) x |= 1 << b[i];
-      idx[c] = sw<R>(x);
+        for (int i = 0; i < G; ++i)
+          if ((c >> i) & 1) x ^= sbit[i];
+        idx[c] = x;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) {
+        int x = base;
+#pragma unroll
+        for (int i = 0; i < G; ++i)
+          if ((c >> i) & 1) x |= 1 << b[i];
+        idx[c] = sw<R>(x);
+      }
     }
 #pragma unroll
     for (int pass = 0; pass < 2; ++pass) {
@@ -588,20 +608,38 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
     ax[i] = d.xy[g0 + i].axis;
     acc[i] = (R)0;
   }
+  int sbit[sizeof(R) == 4 ? G : 1];
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int i = 0; i < G; ++i) sbit[i] = sw<R>(1 << b[i]);
+  }
   const int ntask = tsize >> G;
   for (int tk = threadIdx.x; tk < ntask; tk += NTHREADS) {
     int base = tk;
 #pragma unroll
     for (int i = 0; i < G; ++i) base = insert0(base, b[i]);
     C la[1 << G], qa[1 << G];
+    if constexpr (sizeof(R) == 4) {
+      const int sb = sw<R>(base);
 #pragma unroll
-    for (int c = 0; c < (1 << G); ++c) {
-      int x = base;
+      for (int c = 0; c < (1 << G); ++c) {
+        int x = sb;
 #pragma unroll
-      for (int i = 0; i < G; ++i)
-        if ((c >> i) & 1) x |= 1 << b[i];
-      la[c] = tl[sw<R>(x)];
-      qa[c] = tp[sw<R>(x)];
+        for (int i = 0; i < G; ++i)
+          if ((c >> i) & 1) x ^= sbit[i];
+        la[c] = tl[x];
+        qa[c] = tp[x];
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) {
+        int x = base;
+#pragma unroll
+        for (int i = 0; i < G; ++i)
+          if ((c >> i) & 1) x |= 1 << b[i];
+        la[c] = tl[sw<R>(x)];
+        qa[c] = tp[sw<R>(x)];
+      }
     }
 #pragma unroll
     for (int i = 0; i < G; ++i) {
