@@ -788,6 +788,7 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
   const int64_t ntiles = (int64_t)1 << (n - t);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
+  const bool diag_pass = d.has_diag || d.cost != COST_NONE || d.pre == ENT_CZ;
 
   // copies of one tile into dst: this thread's elements only
   const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts'
@@ -818,7 +819,9 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
     cp_async_wait<1>();   // this thread's copies of the current tile have landed
     const int64_t base = deposit(tileid, S.outside, n - t);
     const int zp = zpt | zpattern((uint64_t)base, d);
-    if (active) {
+    // sweeps without a diagonal, a cost phase or a CZ sign (the later
+    // sweeps of a layer) skip the pass: it would rewrite every element unchanged
+    if (active && diag_pass) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
