@@ -788,7 +788,13 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
   const int64_t ntiles = (int64_t)1 << (n - t);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
-  const bool diag_pass = d.has_diag || d.cost != COST_NONE || d.pre == ENT_CZ;
+  // The cost phase and the CZ sign precede the sweep's rotations and do not
+  // commute with them: a pass over the landed tile applies them (with the
+  // diagonal).  Otherwise the diagonal (Z rotations on qubits the sweep does
+  // not rotate, times the scalar layer scale) commutes with the rotations and
+  // is applied as the tile is stored; sweeps with neither skip the pass.
+  const bool diag_pass = d.cost != COST_NONE || d.pre == ENT_CZ;
+  const bool diag_store = !diag_pass && d.has_diag;
 
   // copies of one tile into dst: this thread's elements only
   const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts'
@@ -819,8 +825,6 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
     cp_async_wait<1>();   // this thread's copies of the current tile have landed
     const int64_t base = deposit(tileid, S.outside, n - t);
     const int zp = zpt | zpattern((uint64_t)base, d);
-    // sweeps without a diagonal, a cost phase or a CZ sign (the later
-    // sweeps of a layer) skip the pass: it would rewrite every element unchanged
     if (active && diag_pass) {
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
@@ -836,7 +840,10 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
         const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-        p.psi_out[x] = tile[sw<R>(e)];
+        const C v = tile[sw<R>(e)];
+        p.psi_out[x] = diag_store ? apply_diag<C>(v, x, zp | S.zpk[k], d, ztab, ctab, p.cost_i, p.cost_d, gamma,
+                                                  fold, false)
+                                  : v;
       }
     }
     __syncthreads();  // the buffer is refilled by the copies issued next iteration
