@@ -816,56 +816,51 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
   const bool diag_pass = d.cost != COST_NONE || d.pre == ENT_CZ;
   const bool diag_store = !diag_pass && d.has_diag;
 
-  // complex64 (issue-bound) takes the cheaper index forms: tile bases by the
-  // masked add; an element's shared-memory slot sw(tid + k NTHREADS) =
-  // sw(tid) + k NTHREADS (the swizzle mixes bits below 8 only); its global
-  // index base | dep_lo | offhi[k] as a per-tile pointer plus offhi[k] (the
-  // parts are disjoint).  complex128, bound by the FP64 pipe, keeps the
-  // direct forms.
+  // Index forms: tile bases by the masked add; an element's shared-memory
+  // slot sw(tid + k NTHREADS) = sw(tid) + k NTHREADS (the swizzle mixes bits
+  // below 8 only); its global index base | dep_lo | offhi[k] as a per-tile
+  // pointer plus offhi[k] (the parts are disjoint).
   TileBases tb(S.outside, n - t, n, d.bits, t);
   const int stid = sw<R>(tid);
 
   // copies of one tile into dst: this thread's elements only
   const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts'
-  auto issue = [&](int64_t tileid, int64_t base, C* dst) {
+  auto issue = [&](int64_t base, C* dst) {
     if (active) {
-      if constexpr (sizeof(R) == 4) {
-        const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
-        const C* pin = p.psi_in + (uint64_t)(base | dep_lo);
-        for (int k = 0; k < nk; ++k)
-          cp_async_elem(&dst[stid + k * NTHREADS],
-                        d.pre == ENT_CNOT ? p.psi_in + (lbase ^ (uint64_t)ladk[k]) : pin + S.offhi[k]);
-      } else {
-        base = deposit(tileid, S.outside, n - t);
-        for (int k = 0; k < nk; ++k) {
-          const int e = tid + k * NTHREADS;
-          const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-          cp_async_elem(&dst[sw<R>(e)], p.psi_in + (d.pre == ENT_CNOT ? ladder_inv(x, lm) : x));
-        }
+      const uint64_t bd = (uint64_t)(base | dep_lo);
+      const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
+      for (int k = 0; k < nk; ++k) {
+        const int64_t oh = S.offhi[k];
+        // the ladder image: complex64 from its parts' images (fewer integer
+        // instructions); complex128 computes it (a shared-memory load costs
+        // more there than integer work)
+        const uint64_t src =
+            sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_inv(bd + (uint64_t)oh, lm);
+        cp_async_elem(&dst[stid + k * NTHREADS], d.pre == ENT_CNOT ? p.psi_in + src : p.psi_in + bd + oh);
       }
     }
     cp_async_commit();
   };
 
   int cur = 0;
-  int64_t bcur = sizeof(R) == 4 ? tb.advance() : 0;
-  if ((int64_t)blockIdx.x < ntiles) issue(blockIdx.x, bcur, buf0);
+  int64_t bcur = tb.advance();
+  if ((int64_t)blockIdx.x < ntiles) issue(bcur, buf0);
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     C* tile = buf0 + cur * tsize;
     const int64_t nxt = tileid + gridDim.x;
-    const int64_t bnext = sizeof(R) == 4 ? tb.advance() : 0;
+    const int64_t bnext = tb.advance();
     if (nxt < ntiles)
-      issue(nxt, bnext, buf0 + (cur ^ 1) * tsize);
+      issue(bnext, buf0 + (cur ^ 1) * tsize);
     else
       cp_async_commit();  // an empty group keeps the count of pending groups uniform
     cp_async_wait<1>();   // this thread's copies of the current tile have landed
-    const int64_t base = sizeof(R) == 4 ? bcur : deposit(tileid, S.outside, n - t);
+    const int64_t base = bcur;
     const uint64_t bd = (uint64_t)(base | dep_lo);
     const int zp = zpt | zpattern((uint64_t)base, d);
     if (active && diag_pass) {
       for (int k = 0; k < nk; ++k) {
-        const int e = sizeof(R) == 4 ? stid + k * NTHREADS : sw<R>(tid + k * NTHREADS);
-        const uint64_t x = sizeof(R) == 4 ? bd + (uint64_t)S.offhi[k] : (uint64_t)(base | dep_lo | S.offhi[k]);
+        const int e = stid + k * NTHREADS;
+        const uint64_t x = bd + (uint64_t)S.offhi[k];
         C v = tile[e];
         if (d.pre == ENT_CZ && cz_negative(x)) v = cneg(v);
         tile[e] = apply_diag<C>(v, x, zp | S.zpk[k], d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
@@ -874,24 +869,13 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
     __syncthreads();
     apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
     if (active) {
-      if constexpr (sizeof(R) == 4) {
-        C* out = p.psi_out + bd;
-        for (int k = 0; k < nk; ++k) {
-          const int64_t oh = S.offhi[k];
-          const C v = tile[stid + k * NTHREADS];
-          out[oh] = diag_store ? apply_diag<C>(v, bd + (uint64_t)oh, zp | S.zpk[k], d, ztab, ctab, p.cost_i,
-                                               p.cost_d, gamma, fold, false)
-                               : v;
-        }
-      } else {
-        for (int k = 0; k < nk; ++k) {
-          const int e = tid + k * NTHREADS;
-          const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-          const C v = tile[sw<R>(e)];
-          p.psi_out[x] = diag_store ? apply_diag<C>(v, x, zp | S.zpk[k], d, ztab, ctab, p.cost_i, p.cost_d, gamma,
-                                                    fold, false)
-                                    : v;
-        }
+      C* out = p.psi_out + bd;
+      for (int k = 0; k < nk; ++k) {
+        const int64_t oh = S.offhi[k];
+        const C v = tile[stid + k * NTHREADS];
+        out[oh] = diag_store ? apply_diag<C>(v, bd + (uint64_t)oh, zp | S.zpk[k], d, ztab, ctab, p.cost_i,
+                                             p.cost_d, gamma, fold, false)
+                             : v;
       }
     }
     __syncthreads();  // the buffer is refilled by the copies issued next iteration
@@ -963,16 +947,14 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   R Uk[5] = {(R)0, (R)0, (R)0, (R)0, (R)0};
   bool any_base = false;
   for (int j = 0; j < d.nz; ++j) any_base |= S.zk[j] == -2;
-  // complex64 (issue-bound) takes the cheaper index forms: tile bases by the
-  // masked add; an element's shared-memory slot sw(tid + k NTHREADS) =
-  // sw(tid) + k NTHREADS (the swizzle mixes bits below 8 only); its global
-  // index base | dep_lo | offhi[k] as a per-tile pointer plus offhi[k] (the
-  // parts are disjoint).  complex128, bound by the FP64 pipe, keeps the
-  // direct forms.
+  // Index forms: tile bases by the masked add; an element's shared-memory
+  // slot sw(tid + k NTHREADS) = sw(tid) + k NTHREADS (the swizzle mixes bits
+  // below 8 only); its global index base | dep_lo | offhi[k] as a per-tile
+  // pointer plus offhi[k] (the parts are disjoint).
   TileBases tb(S.outside, n - t, n, d.bits, t);
   const int stid = sw<R>(tid);
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
-    const int64_t base = sizeof(R) == 4 ? tb.advance() : deposit(tileid, S.outside, n - t);
+    const int64_t base = tb.advance();
     const uint64_t bd = (uint64_t)(base | dep_lo);
     const int zp = zpt | zpattern((uint64_t)base, d);
     const uint64_t lbase = ladder_fwd((uint64_t)base, lm) ^ ldep;
@@ -981,31 +963,25 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       // all of this thread's loads of the tile in flight at once (asynchronous
       // global->shared copies), then one wait: a load-use loop would wait one
       // memory round trip per element
-      if constexpr (sizeof(R) == 4) {
-        const C* lin = p.lam_in + bd;
-        const C* pin = p.psi_in + bd;
-        for (int k = 0; k < nk; ++k) {
-          const int64_t oh = S.offhi[k];
-          // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y]
-          const uint64_t ax = lbase ^ (uint64_t)ladk[k];
-          cp_async_elem(&tl[stid + k * NTHREADS], d.lam_undo == ENT_CNOT ? p.lam_in + ax : lin + oh);
-          cp_async_elem(&tp[stid + k * NTHREADS], d.psi_undo == ENT_CNOT ? p.psi_in + ax : pin + oh);
-        }
-      } else {
-        for (int k = 0; k < nk; ++k) {
-          const int e = tid + k * NTHREADS;
-          const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-          cp_async_elem(&tl[sw<R>(e)], p.lam_in + (d.lam_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
-          cp_async_elem(&tp[sw<R>(e)], p.psi_in + (d.psi_undo == ENT_CNOT ? ladder_fwd(x, lm) : x));
-        }
+      const C* lin = p.lam_in + bd;
+      const C* pin = p.psi_in + bd;
+      for (int k = 0; k < nk; ++k) {
+        const int64_t oh = S.offhi[k];
+        // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y];
+        // complex64 takes the image from its parts' images (fewer integer
+        // instructions), complex128 computes it (a shared-memory load costs
+        // more there than integer work)
+        const uint64_t ax = sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_fwd(bd + (uint64_t)oh, lm);
+        cp_async_elem(&tl[stid + k * NTHREADS], d.lam_undo == ENT_CNOT ? p.lam_in + ax : lin + oh);
+        cp_async_elem(&tp[stid + k * NTHREADS], d.psi_undo == ENT_CNOT ? p.psi_in + ax : pin + oh);
       }
       cp_async_commit();
       cp_async_wait<0>();
       const bool cz_l = d.lam_undo == ENT_CZ, cz_p = d.psi_undo == ENT_CZ;
       if (need_w || cz_l || cz_p) {
         for (int k = 0; k < nk; ++k) {
-          const int e = sizeof(R) == 4 ? stid + k * NTHREADS : sw<R>(tid + k * NTHREADS);
-          const uint64_t x = sizeof(R) == 4 ? bd + (uint64_t)S.offhi[k] : (uint64_t)(base | dep_lo | S.offhi[k]);
+          const int e = stid + k * NTHREADS;
+          const uint64_t x = bd + (uint64_t)S.offhi[k];
           C l = tl[e];
           C q = tp[e];
           const bool neg = (cz_l || cz_p) && cz_negative(x);
@@ -1058,30 +1034,17 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     // inverse rotations (they commute, so the group order is free)
     apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
     if (active) {
-      if constexpr (sizeof(R) == 4) {
-        C* lout = p.lam_out + bd;
-        C* pout = p.psi_out + bd;
-        for (int k = 0; k < nk; ++k) {
-          const int e = stid + k * NTHREADS;
-          const int64_t oh = S.offhi[k];
-          const uint64_t x = bd + (uint64_t)oh;
-          const int zpe = zp | S.zpk[k];
-          lout[oh] = apply_diag<C>(tl[e], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true);
-          if (UNCOMPUTE)
-            pout[oh] = cscale(apply_diag<C>(tp[e], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true),
-                              psi_mult);
-        }
-      } else {
-        for (int k = 0; k < nk; ++k) {
-          const int e = tid + k * NTHREADS;
-          const uint64_t x = (uint64_t)(base | dep_lo | S.offhi[k]);
-          const int zpe = zp | S.zpk[k];
-          p.lam_out[x] = apply_diag<C>(tl[sw<R>(e)], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true);
-          if (UNCOMPUTE)
-            p.psi_out[x] = cscale(apply_diag<C>(tp[sw<R>(e)], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma,
-                                                fold, true),
-                                  psi_mult);
-        }
+      C* lout = p.lam_out + bd;
+      C* pout = p.psi_out + bd;
+      for (int k = 0; k < nk; ++k) {
+        const int e = stid + k * NTHREADS;
+        const int64_t oh = S.offhi[k];
+        const uint64_t x = bd + (uint64_t)oh;
+        const int zpe = zp | S.zpk[k];
+        lout[oh] = apply_diag<C>(tl[e], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true);
+        if (UNCOMPUTE)
+          pout[oh] = cscale(apply_diag<C>(tp[e], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true),
+                            psi_mult);
       }
     }
     __syncthreads();
