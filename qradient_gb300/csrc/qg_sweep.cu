@@ -978,7 +978,28 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       cp_async_commit();
       cp_async_wait<0>();
       const bool cz_l = d.lam_undo == ENT_CZ, cz_p = d.psi_undo == ENT_CZ;
-      if (need_w || cz_l || cz_p) {
+      if (sizeof(R) == 4 && need_w && !cz_l && !cz_p && d.gslot < 0 && nk >= 4) {
+        // complex64, Z sums only: four elements at a time, so that bits 0 and
+        // 1 of k are fixed per element and bits 2..4 tested once per four
+        // (every U_k is accumulated; those without a Z rotation go unread)
+        for (int k0 = 0; k0 < nk; k0 += 4) {
+          R w[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const C l = tl[stid + (k0 + c) * NTHREADS];
+            const C q = tp[stid + (k0 + c) * NTHREADS];
+            w[c] = fma(l.x, q.y, -l.y * q.x);  // Im(conj(l) q)
+          }
+          const R w13 = w[1] + w[3], w23 = w[2] + w[3];
+          const R s4 = (w[0] + w[2]) + w13;
+          tT += s4;
+          Uk[0] += w13;
+          Uk[1] += w23;
+          if (k0 & 4) Uk[2] += s4;
+          if (k0 & 8) Uk[3] += s4;
+          if (k0 & 16) Uk[4] += s4;
+        }
+      } else if (need_w || cz_l || cz_p) {
         for (int k = 0; k < nk; ++k) {
           const int e = stid + k * NTHREADS;
           const uint64_t x = bd + (uint64_t)S.offhi[k];
