@@ -828,15 +828,24 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
   auto issue = [&](int64_t base, C* dst) {
     if (active) {
       const uint64_t bd = (uint64_t)(base | dep_lo);
-      const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
-      for (int k = 0; k < nk; ++k) {
-        const int64_t oh = S.offhi[k];
-        // the ladder image: complex64 from its parts' images (fewer integer
-        // instructions); complex128 computes it (a shared-memory load costs
-        // more there than integer work)
-        const uint64_t src =
-            sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_inv(bd + (uint64_t)oh, lm);
-        cp_async_elem(&dst[stid + k * NTHREADS], d.pre == ENT_CNOT ? p.psi_in + src : p.psi_in + bd + oh);
+      // complex64 (issue-bound) has a loop per case and takes the ladder
+      // image from its parts' images; complex128 (FP64-bound) one loop that
+      // computes the image (a shared-memory load costs more there than
+      // integer work)
+      if constexpr (sizeof(R) == 4) {
+        if (d.pre == ENT_CNOT) {
+          const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
+          for (int k = 0; k < nk; ++k) cp_async_elem(&dst[stid + k * NTHREADS], p.psi_in + (lbase ^ (uint64_t)ladk[k]));
+        } else {
+          const C* pin = p.psi_in + bd;
+          for (int k = 0; k < nk; ++k) cp_async_elem(&dst[stid + k * NTHREADS], pin + S.offhi[k]);
+        }
+      } else {
+        for (int k = 0; k < nk; ++k) {
+          const int64_t oh = S.offhi[k];
+          cp_async_elem(&dst[stid + k * NTHREADS],
+                        d.pre == ENT_CNOT ? p.psi_in + ladder_inv(bd + (uint64_t)oh, lm) : p.psi_in + bd + oh);
+        }
       }
     }
     cp_async_commit();
@@ -870,12 +879,16 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
     apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
     if (active) {
       C* out = p.psi_out + bd;
-      for (int k = 0; k < nk; ++k) {
-        const int64_t oh = S.offhi[k];
-        const C v = tile[stid + k * NTHREADS];
-        out[oh] = diag_store ? apply_diag<C>(v, bd + (uint64_t)oh, zp | S.zpk[k], d, ztab, ctab, p.cost_i,
-                                             p.cost_d, gamma, fold, false)
-                             : v;
+      if (sizeof(R) == 8 || diag_store) {
+        for (int k = 0; k < nk; ++k) {
+          const int64_t oh = S.offhi[k];
+          const C v = tile[stid + k * NTHREADS];
+          out[oh] = diag_store ? apply_diag<C>(v, bd + (uint64_t)oh, zp | S.zpk[k], d, ztab, ctab, p.cost_i,
+                                               p.cost_d, gamma, fold, false)
+                               : v;
+        }
+      } else {
+        for (int k = 0; k < nk; ++k) out[S.offhi[k]] = tile[stid + k * NTHREADS];
       }
     }
     __syncthreads();  // the buffer is refilled by the copies issued next iteration
@@ -965,15 +978,23 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       // memory round trip per element
       const C* lin = p.lam_in + bd;
       const C* pin = p.psi_in + bd;
-      for (int k = 0; k < nk; ++k) {
-        const int64_t oh = S.offhi[k];
-        // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y];
-        // complex64 takes the image from its parts' images (fewer integer
-        // instructions), complex128 computes it (a shared-memory load costs
-        // more there than integer work)
-        const uint64_t ax = sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_fwd(bd + (uint64_t)oh, lm);
-        cp_async_elem(&tl[stid + k * NTHREADS], d.lam_undo == ENT_CNOT ? p.lam_in + ax : lin + oh);
-        cp_async_elem(&tp[stid + k * NTHREADS], d.psi_undo == ENT_CNOT ? p.psi_in + ax : pin + oh);
+      if (sizeof(R) == 4 && d.lam_undo != ENT_CNOT && d.psi_undo != ENT_CNOT) {
+        for (int k = 0; k < nk; ++k) {
+          const int64_t oh = S.offhi[k];
+          cp_async_elem(&tl[stid + k * NTHREADS], lin + oh);
+          cp_async_elem(&tp[stid + k * NTHREADS], pin + oh);
+        }
+      } else {
+        for (int k = 0; k < nk; ++k) {
+          const int64_t oh = S.offhi[k];
+          // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y];
+          // complex64 takes the image from its parts' images (fewer integer
+          // instructions), complex128 computes it (a shared-memory load costs
+          // more there than integer work)
+          const uint64_t ax = sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_fwd(bd + (uint64_t)oh, lm);
+          cp_async_elem(&tl[stid + k * NTHREADS], d.lam_undo == ENT_CNOT ? p.lam_in + ax : lin + oh);
+          cp_async_elem(&tp[stid + k * NTHREADS], d.psi_undo == ENT_CNOT ? p.psi_in + ax : pin + oh);
+        }
       }
       cp_async_commit();
       cp_async_wait<0>();
@@ -1054,7 +1075,11 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     __syncthreads();
     // inverse rotations (they commute, so the group order is free)
     apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
-    if (active) {
+    if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
+      // nothing diagonal to apply and no psi to write: a plain copy-out
+      C* lout = p.lam_out + bd;
+      for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = tl[stid + k * NTHREADS];
+    } else if (active) {
       C* lout = p.lam_out + bd;
       C* pout = p.psi_out + bd;
       for (int k = 0; k < nk; ++k) {
