@@ -15,6 +15,10 @@
 
 namespace qg {
 
+// default complex64 tile bits (the size the sweep kernels are also
+// instantiated for with the tile size fixed at compile time)
+constexpr int kTileC64 = 12;
+
 // ---------------------------------------------------------------- helpers
 
 __device__ __forceinline__ double angle_of(const AngleRef& a, const double* params) {
@@ -785,13 +789,18 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-template <typename R>
+// TB > 0: an instantiation for tiles of exactly TB bits (the launcher picks
+// it when d.t == TB), so that the tile size, the element-loop count and the
+// offset between the two tile buffers are compile-time constants: element
+// loops unroll and shared-memory offsets become immediates.  TB = 0 takes
+// the tile size from the descriptor.
+template <typename R, int TB>
 __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pipe_kernel(const __grid_constant__ SweepDesc d,
                                                                   SweepPtrs<R> p) {
   using C = typename C2T<R>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SetupShared S;
-  const int t = d.t, n = d.n;
+  const int t = TB > 0 ? TB : d.t, n = d.n;
   const int tsize = 1 << t;
   C* buf0 = (C*)smem;
   C* ztab = buf0 + 2 * tsize;
@@ -913,12 +922,12 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pi
 
 // At least 3 resident CTAs per SM for complex64 (its two tiles take 72 KB
 // of shared memory) and 2 for complex128: caps registers at 85 / 128.
-template <typename R, bool UNCOMPUTE>
+template <typename R, bool UNCOMPUTE, int TB>
 __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_kernel(const __grid_constant__ SweepDesc d, SweepPtrs<R> p) {
   using C = typename C2T<R>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SetupShared S;
-  const int t = d.t, n = d.n;
+  const int t = TB > 0 ? TB : d.t, n = d.n;
   const int tsize = 1 << t;
   C* tl = (C*)smem;
   C* tp = tl + tsize;
@@ -1382,17 +1391,46 @@ cudaError_t prepare_sweep_kernels() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const void* fns[] = {(const void*)sweep_fwd_kernel<double>,          (const void*)sweep_fwd_kernel<float>,
-                       (const void*)sweep_fwd_pipe_kernel<double>,     (const void*)sweep_fwd_pipe_kernel<float>,
-                       (const void*)sweep_bwd_kernel<double, false>,   (const void*)sweep_bwd_kernel<double, true>,
-                       (const void*)sweep_bwd_kernel<float, false>,    (const void*)sweep_bwd_kernel<float, true>,
-                       (const void*)observable_kernel<double>,         (const void*)observable_kernel<float>};
+  const void* fns[] = {(const void*)sweep_fwd_kernel<double>,
+                       (const void*)sweep_fwd_kernel<float>,
+                       (const void*)sweep_fwd_pipe_kernel<double, 0>,
+                       (const void*)sweep_fwd_pipe_kernel<float, 0>,
+                       (const void*)sweep_fwd_pipe_kernel<float, kTileC64>,
+                       (const void*)sweep_bwd_kernel<double, false, 0>,
+                       (const void*)sweep_bwd_kernel<double, true, 0>,
+                       (const void*)sweep_bwd_kernel<float, false, 0>,
+                       (const void*)sweep_bwd_kernel<float, true, 0>,
+                       (const void*)sweep_bwd_kernel<float, false, kTileC64>,
+                       (const void*)sweep_bwd_kernel<float, true, kTileC64>,
+                       (const void*)observable_kernel<double>,
+                       (const void*)observable_kernel<float>};
   for (const void* fn : fns) {
     e = set_smem_limit(fn, optin);
     if (e != cudaSuccess) return e;
   }
   ready[dev].store(1, std::memory_order_release);
   return cudaSuccess;
+}
+
+// The kernel a sweep launches: complex64 sweeps over tiles of the default
+// size take the instantiation with the tile size fixed at compile time.
+template <typename R>
+static bool fixed_tile(const SweepDesc& d) {
+  return sizeof(R) == 4 && d.t == kTileC64;
+}
+template <typename R>
+static const void* fwd_pipe_fn(const SweepDesc& d) {
+  if constexpr (sizeof(R) == 4)
+    if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<R, kTileC64>;
+  return (const void*)sweep_fwd_pipe_kernel<R, 0>;
+}
+template <typename R>
+static const void* bwd_fn(const SweepDesc& d, bool uncompute) {
+  if constexpr (sizeof(R) == 4)
+    if (fixed_tile<R>(d))
+      return uncompute ? (const void*)sweep_bwd_kernel<R, true, kTileC64>
+                       : (const void*)sweep_bwd_kernel<R, false, kTileC64>;
+  return uncompute ? (const void*)sweep_bwd_kernel<R, true, 0> : (const void*)sweep_bwd_kernel<R, false, 0>;
 }
 
 template <typename R>
@@ -1404,14 +1442,8 @@ int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe) {
     cudaGetLastError();
     return 1;
   }
-  if (!bwd && pipe)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_pipe_kernel<R>, NTHREADS, smem);
-  else if (!bwd)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_fwd_kernel<R>, NTHREADS, smem);
-  else if (uncompute)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, true>, NTHREADS, smem);
-  else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sweep_bwd_kernel<R, false>, NTHREADS, smem);
+  const void* fn = !bwd && pipe ? fwd_pipe_fn<R>(d) : !bwd ? (const void*)sweep_fwd_kernel<R> : bwd_fn<R>(d, uncompute);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, NTHREADS, smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -1427,7 +1459,12 @@ cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   if (pipe && d.start == START_LOAD) {
-    sweep_fwd_pipe_kernel<R><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
+    if constexpr (sizeof(R) == 4)
+      if (fixed_tile<R>(d)) {
+        sweep_fwd_pipe_kernel<R, kTileC64><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
+        return cudaGetLastError();
+      }
+    sweep_fwd_pipe_kernel<R, 0><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
     return cudaGetLastError();
   }
   sweep_fwd_kernel<R><<<grid, NTHREADS, sweep_smem<R>(d, false), st>>>(d, p);
@@ -1439,10 +1476,18 @@ cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool unc
   const size_t smem = sweep_smem<R>(d, true);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
+  if constexpr (sizeof(R) == 4)
+    if (fixed_tile<R>(d)) {
+      if (uncompute)
+        sweep_bwd_kernel<R, true, kTileC64><<<grid, NTHREADS, smem, st>>>(d, p);
+      else
+        sweep_bwd_kernel<R, false, kTileC64><<<grid, NTHREADS, smem, st>>>(d, p);
+      return cudaGetLastError();
+    }
   if (uncompute)
-    sweep_bwd_kernel<R, true><<<grid, NTHREADS, smem, st>>>(d, p);
+    sweep_bwd_kernel<R, true, 0><<<grid, NTHREADS, smem, st>>>(d, p);
   else
-    sweep_bwd_kernel<R, false><<<grid, NTHREADS, smem, st>>>(d, p);
+    sweep_bwd_kernel<R, false, 0><<<grid, NTHREADS, smem, st>>>(d, p);
   return cudaGetLastError();
 }
 
