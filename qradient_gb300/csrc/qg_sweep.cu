@@ -15,9 +15,11 @@
 
 namespace qg {
 
-// default complex64 tile bits (the size the sweep kernels are also
-// instantiated for with the tile size fixed at compile time)
-constexpr int kTileC64 = 12;
+// default tile bits (the sizes the sweep kernels are also instantiated for
+// with the tile size fixed at compile time)
+constexpr int kTileC64 = 12, kTileC128 = 11;
+template <typename R>
+constexpr int kTileFixed = sizeof(R) == 4 ? kTileC64 : kTileC128;
 
 // ---------------------------------------------------------------- helpers
 
@@ -1396,12 +1398,15 @@ cudaError_t prepare_sweep_kernels() {
                        (const void*)sweep_fwd_pipe_kernel<double, 0>,
                        (const void*)sweep_fwd_pipe_kernel<float, 0>,
                        (const void*)sweep_fwd_pipe_kernel<float, kTileC64>,
+                       (const void*)sweep_fwd_pipe_kernel<double, kTileC128>,
                        (const void*)sweep_bwd_kernel<double, false, 0>,
                        (const void*)sweep_bwd_kernel<double, true, 0>,
                        (const void*)sweep_bwd_kernel<float, false, 0>,
                        (const void*)sweep_bwd_kernel<float, true, 0>,
                        (const void*)sweep_bwd_kernel<float, false, kTileC64>,
                        (const void*)sweep_bwd_kernel<float, true, kTileC64>,
+                       (const void*)sweep_bwd_kernel<double, false, kTileC128>,
+                       (const void*)sweep_bwd_kernel<double, true, kTileC128>,
                        (const void*)observable_kernel<double>,
                        (const void*)observable_kernel<float>};
   for (const void* fn : fns) {
@@ -1412,24 +1417,22 @@ cudaError_t prepare_sweep_kernels() {
   return cudaSuccess;
 }
 
-// The kernel a sweep launches: complex64 sweeps over tiles of the default
-// size take the instantiation with the tile size fixed at compile time.
+// The kernel a sweep launches: sweeps over tiles of the default size take
+// the instantiation with the tile size fixed at compile time.
 template <typename R>
 static bool fixed_tile(const SweepDesc& d) {
-  return sizeof(R) == 4 && d.t == kTileC64;
+  return d.t == kTileFixed<R>;
 }
 template <typename R>
 static const void* fwd_pipe_fn(const SweepDesc& d) {
-  if constexpr (sizeof(R) == 4)
-    if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<R, kTileC64>;
+  if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<R, kTileFixed<R>>;
   return (const void*)sweep_fwd_pipe_kernel<R, 0>;
 }
 template <typename R>
 static const void* bwd_fn(const SweepDesc& d, bool uncompute) {
-  if constexpr (sizeof(R) == 4)
-    if (fixed_tile<R>(d))
-      return uncompute ? (const void*)sweep_bwd_kernel<R, true, kTileC64>
-                       : (const void*)sweep_bwd_kernel<R, false, kTileC64>;
+  if (fixed_tile<R>(d))
+    return uncompute ? (const void*)sweep_bwd_kernel<R, true, kTileFixed<R>>
+                     : (const void*)sweep_bwd_kernel<R, false, kTileFixed<R>>;
   return uncompute ? (const void*)sweep_bwd_kernel<R, true, 0> : (const void*)sweep_bwd_kernel<R, false, 0>;
 }
 
@@ -1459,11 +1462,10 @@ cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   if (pipe && d.start == START_LOAD) {
-    if constexpr (sizeof(R) == 4)
-      if (fixed_tile<R>(d)) {
-        sweep_fwd_pipe_kernel<R, kTileC64><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
-        return cudaGetLastError();
-      }
+    if (fixed_tile<R>(d)) {
+      sweep_fwd_pipe_kernel<R, kTileFixed<R>><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
+      return cudaGetLastError();
+    }
     sweep_fwd_pipe_kernel<R, 0><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
     return cudaGetLastError();
   }
@@ -1476,14 +1478,13 @@ cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool unc
   const size_t smem = sweep_smem<R>(d, true);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
-  if constexpr (sizeof(R) == 4)
-    if (fixed_tile<R>(d)) {
-      if (uncompute)
-        sweep_bwd_kernel<R, true, kTileC64><<<grid, NTHREADS, smem, st>>>(d, p);
-      else
-        sweep_bwd_kernel<R, false, kTileC64><<<grid, NTHREADS, smem, st>>>(d, p);
-      return cudaGetLastError();
-    }
+  if (fixed_tile<R>(d)) {
+    if (uncompute)
+      sweep_bwd_kernel<R, true, kTileFixed<R>><<<grid, NTHREADS, smem, st>>>(d, p);
+    else
+      sweep_bwd_kernel<R, false, kTileFixed<R>><<<grid, NTHREADS, smem, st>>>(d, p);
+    return cudaGetLastError();
+  }
   if (uncompute)
     sweep_bwd_kernel<R, true, 0><<<grid, NTHREADS, smem, st>>>(d, p);
   else
