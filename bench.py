@@ -555,13 +555,16 @@ def main():
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     traffic = None
     pipe_busy = None
+    # DRAM bytes per backward launch from an ncu capture of the same dtype and
+    # qubit count (null for other workloads)
     tpath = os.path.join(ROOT, "profiles", "backward_sweep_traffic.json")
     if os.path.exists(tpath):
         try:
-            prof = json.load(open(tpath))
-            traffic = prof.get("dram_bytes_per_launch")
-            pipe_busy = prof.get("fp64_pipe_busy_ncu")
-        except ValueError:
+            prof = json.load(open(tpath)).get(args.dtype) or {}
+            if prof.get("n") == args.n:
+                traffic = prof.get("dram_bytes_per_launch")
+                pipe_busy = prof.get("fp64_pipe_busy_ncu")
+        except (ValueError, AttributeError):
             traffic = None
     if args.dtype == "complex128":
         roof = {"bound": "fp64", "kernel": "sweep_bwd_kernel<double,history>", "achieved": achieved_tflops,
