@@ -796,8 +796,11 @@ __device__ __forceinline__ void cp_async_wait() {
 // offset between the two tile buffers are compile-time constants: element
 // loops unroll and shared-memory offsets become immediates.  TB = 0 takes
 // the tile size from the descriptor.
+// Three resident CTAs per SM in both precisions (registers capped at 85):
+// a complex128 forward sweep with few rotations per amplitude is short of
+// FP64 work to overlap its tile loads with, and more CTAs give more.
 template <typename R, int TB>
-__global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_fwd_pipe_kernel(const __grid_constant__ SweepDesc d,
+__global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __grid_constant__ SweepDesc d,
                                                                   SweepPtrs<R> p) {
   using C = typename C2T<R>::T;
   extern __shared__ __align__(16) unsigned char smem[];
