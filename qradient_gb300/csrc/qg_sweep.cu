@@ -1157,6 +1157,36 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
 // lam = O psi for O = sum of weighted Pauli terms (observable.py:45-73), and
 // the partial sums of Re<psi|lam> (base.py:17-20).  X/Y terms need the
 // partner amplitude and are taken from the staged tile.
+//
+// Diagonal terms (Z, ZZ): an element index x = base | dep_lo | offhi[k] has
+// three disjoint parts, so a term's sign (-1)^{popc(x & m)} is the sign on
+// base | dep_lo (fixed per thread and tile) times the sign on offhi[k]
+// (which depends only on the k bits the mask covers).  Per thread and tile
+// the terms are summed into b[S], S = the subset of element-loop bits the
+// mask covers, and a Walsh-Hadamard transform over those bits gives the
+// diagonal of all the thread's elements at once:
+//   D(k) = sum_S b[S] (-1)^{popc(S & k)}.
+// Per-term work is then per thread and tile, not per element, and integer
+// work: the terms of a subset keep the host's order by weight, so the signs
+// of a run of equal weights are counted and multiplied once (bit 63 of a
+// stored mask marks the last term of a run).  Up to OBS_KBITS element-loop
+// bits (16 elements per thread); larger tiles take the per-element loop.
+
+constexpr int OBS_KBITS = 4;
+constexpr uint64_t OBS_RUN_END = 1ull << 63;
+
+// Shared-memory layout of the observable kernel after the tile: the thread's
+// diagonal values D(k) (one slot per element), then the diagonal terms
+// ordered by their k subset (masks, weights) and the subset boundaries.
+template <typename R>
+struct ObsSmem {
+  static size_t bytes(int t, int ndiag) {
+    using C = typename C2T<R>::T;
+    const size_t tile = ((size_t)1 << t) * sizeof(C);
+    const size_t dvals = ((size_t)1 << t) * sizeof(R);
+    return tile + dvals + (size_t)ndiag * (sizeof(uint64_t) + sizeof(R)) + ((1 << OBS_KBITS) + 1) * sizeof(int);
+  }
+};
 
 template <typename R>
 __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_constant__ ObsDesc d, const typename C2T<R>::T* psi,
@@ -1170,7 +1200,13 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
   const int t = d.t, n = d.n;
   const int tsize = 1 << t;
   C* tile = (C*)smem;
+  R* dval = (R*)(tile + tsize);                   // D(k) of this thread at dval[k * NTHREADS + tid]
+  uint64_t* tmask = (uint64_t*)(dval + tsize);    // diagonal terms ordered by k subset
+  R* tw = (R*)(tmask + d.ndiag);
+  int* tstart = (int*)(tw + d.ndiag);             // subset S: terms [tstart[S], tstart[S + 1])
   const int tid = threadIdx.x;
+  const int kb = t > 8 ? t - 8 : 0;               // element-loop bits
+  const bool wht = d.ndiag > 0 && d.cost == COST_NONE && kb <= OBS_KBITS;
   if (t > 8) {
     for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) offhi[k] = deposit((int64_t)k << 8, d.bits, t);
   } else if (tid == 0) {
@@ -1184,6 +1220,29 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
       else
         outside[o++] = (uint8_t)b;
     }
+    if (wht) {
+      // counting sort of the diagonal terms by the k bits their mask covers
+      int cnt[(1 << OBS_KBITS) + 1] = {0};
+      auto subset = [&](const ObsTerm& tm) {
+        const uint64_t m = (1ull << tm.b0) | (tm.kind == 3 ? (1ull << tm.b1) : 0ull);
+        int sbits = 0;
+        for (int i = 0; i < kb; ++i) sbits |= (int)((m >> d.bits[8 + i]) & 1) << i;
+        return sbits;
+      };
+      for (int i = 0; i < d.ndiag; ++i) ++cnt[subset(d.term[i]) + 1];
+      for (int sb = 0; sb < (1 << OBS_KBITS); ++sb) cnt[sb + 1] += cnt[sb];
+      for (int sb = 0; sb <= (1 << OBS_KBITS); ++sb) tstart[sb] = cnt[sb];
+      for (int i = 0; i < d.ndiag; ++i) {
+        const ObsTerm& tm = d.term[i];
+        const int pos = cnt[subset(tm)]++;
+        tmask[pos] = (1ull << tm.b0) | (tm.kind == 3 ? (1ull << tm.b1) : 0ull);
+        tw[pos] = sizeof(R) == 4 ? (R)tm.wf : (R)tm.w;
+      }
+      // the last term of each run of equal weights within a subset
+      for (int sb = 0; sb < (1 << OBS_KBITS); ++sb)
+        for (int j = tstart[sb]; j < tstart[sb + 1]; ++j)
+          if (j + 1 == tstart[sb + 1] || tw[j + 1] != tw[j]) tmask[j] |= OBS_RUN_END;
+    }
   }
   __syncthreads();
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
@@ -1191,22 +1250,56 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int64_t ntiles = (int64_t)1 << (n - t);
   const LadderMasks lm = ladder_masks(n);
+  TileBases tb(outside, n - t, n, d.bits, t);
+  const int stid = sw<R>(tid);
   double eacc = 0.0;
   const R w0r = (R)d.cost_w0;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
-    const int64_t base = deposit(tileid, outside, n - t);
+    const int64_t base = tb.advance();
+    const uint64_t bd = (uint64_t)(base | dep_lo);
     if (active) {
       // every load of this thread's elements in flight at once, then one wait
       for (int k = 0; k < nk; ++k) {
-        const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
-        cp_async_elem(&tile[sw<R>(tid + k * NTHREADS)], psi + (d.pre == ENT_CNOT ? ladder_inv(x, lm) : x));
+        const uint64_t x = bd + (uint64_t)offhi[k];
+        cp_async_elem(&tile[stid + k * NTHREADS], psi + (d.pre == ENT_CNOT ? ladder_inv(x, lm) : x));
       }
       cp_async_commit();
+      if (wht) {
+        // the diagonal of this thread's elements while the loads land
+        R b[1 << OBS_KBITS];
+#pragma unroll
+        for (int sb = 0; sb < (1 << OBS_KBITS); ++sb) {
+          R acc = (R)0;
+          int cnt = 0;
+          for (int j = tstart[sb]; j < tstart[sb + 1]; ++j) {
+            const uint64_t m = tmask[j];
+            cnt += 1 - 2 * (__popcll(bd & m) & 1);  // bit 63 lies above every index bit
+            if (m & OBS_RUN_END) {
+              acc = fma(tw[j], (R)cnt, acc);
+              cnt = 0;
+            }
+          }
+          b[sb] = acc;
+        }
+        // butterflies over the kb element-loop bits, on the nk values in use
+#pragma unroll
+        for (int i = 0; i < OBS_KBITS; ++i)
+#pragma unroll
+          for (int k = 0; k < (1 << OBS_KBITS); ++k)
+            if (!((k >> i) & 1) && i < kb && (k | (1 << i)) < nk) {
+              const R u = b[k], v = b[k | (1 << i)];
+              b[k] = u + v;
+              b[k | (1 << i)] = u - v;
+            }
+#pragma unroll
+        for (int k = 0; k < (1 << OBS_KBITS); ++k)
+          if (k < nk) dval[k * NTHREADS + tid] = b[k];
+      }
       cp_async_wait<0>();
       if (d.pre == ENT_CZ)
         for (int k = 0; k < nk; ++k) {
-          const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
-          if (cz_negative(x)) tile[sw<R>(tid + k * NTHREADS)] = cneg(tile[sw<R>(tid + k * NTHREADS)]);
+          const uint64_t x = bd + (uint64_t)offhi[k];
+          if (cz_negative(x)) tile[stid + k * NTHREADS] = cneg(tile[stid + k * NTHREADS]);
         }
     }
     if (d.nxy > 0) __syncthreads();  // X/Y terms read partners other threads loaded
@@ -1214,8 +1307,8 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
       R tacc = (R)0;
       for (int k = 0; k < nk; ++k) {
         const int e = tid + k * NTHREADS;
-        const uint64_t x = (uint64_t)(base | dep_lo | offhi[k]);
-        const C v = tile[sw<R>(e)];
+        const uint64_t x = bd + (uint64_t)offhi[k];
+        const C v = tile[stid + k * NTHREADS];
         // per-amplitude arithmetic in the state's precision (a double
         // instruction in the complex64 kernel costs 16 cycles of the FP64
         // pipe per warp); the expectation is accumulated in double per tile
@@ -1226,6 +1319,8 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
             dv = w0r * (R)cost_i[x];
           } else if (d.cost == COST_REAL) {
             dv = (R)cost_d[x];
+          } else if (wht) {
+            dv = dval[k * NTHREADS + tid];
           } else {
             // integer sign sums per run of equal weights, one multiply per
             // run: the inner loop is integer only, so the compiler cannot
@@ -1499,8 +1594,7 @@ template <typename R>
 cudaError_t launch_observable(const ObsDesc& d, const typename C2T<R>::T* psi, typename C2T<R>::T* lam,
                               const int32_t* cost_i, const double* cost_d, double* partials, int G, int grid,
                               cudaStream_t st) {
-  using C = typename C2T<R>::T;
-  const size_t smem = ((size_t)1 << d.t) * sizeof(C);
+  const size_t smem = ObsSmem<R>::bytes(d.t, d.ndiag);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   observable_kernel<R><<<grid, NTHREADS, smem, st>>>(d, psi, lam, cost_i, cost_d, partials, G);
