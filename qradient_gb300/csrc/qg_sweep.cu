@@ -891,7 +891,11 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
     }
     __syncthreads();
     apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
-    if (active) {
+    if (sizeof(R) == 4 && active && diag_store && d.cost == COST_NONE && d.nz > 0) {
+      // complex64, the merged Z table alone: no per-element case tests
+      C* out = p.psi_out + bd;
+      for (int k = 0; k < nk; ++k) out[S.offhi[k]] = cmul(tile[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
+    } else if (active) {
       C* out = p.psi_out + bd;
       if (sizeof(R) == 8 || diag_store) {
         for (int k = 0; k < nk; ++k) {
@@ -1093,6 +1097,10 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       // nothing diagonal to apply and no psi to write: a plain copy-out
       C* lout = p.lam_out + bd;
       for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = tl[stid + k * NTHREADS];
+    } else if (sizeof(R) == 4 && active && !UNCOMPUTE && d.has_diag && d.cost == COST_NONE && d.nz > 0) {
+      // complex64, the merged Z table alone: no per-element case tests
+      C* lout = p.lam_out + bd;
+      for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = cmul(tl[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
     } else if (active) {
       C* lout = p.lam_out + bd;
       C* pout = p.psi_out + bd;

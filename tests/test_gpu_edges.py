@@ -133,3 +133,29 @@ def test_term_count_limit_is_an_error_not_a_fault():
     c = McClean(n, {"zz": zz}, 1, axes=np.zeros((1, n), dtype=int), angles=np.zeros((1, n)))
     with pytest.raises(_lib.QgradError):
         c.native()
+
+
+@pytest.mark.parametrize("dtype,tol,tiles", [("complex128", 1e-12, (0, 12, 5)), ("complex64", 2e-5, (0, 13, 6))])
+def test_dense_diagonal_observable(dtype, tol, tiles):
+    """Every ZZ pair and every Z term of 14 qubits, weights drawn from a few
+    values (runs of equal weights inside the observable pass's term subsets),
+    through the per-tile term sums (default tiles), the per-element term loop
+    (13-bit complex64 tiles) and small tiles."""
+    n, L = 14, 3
+    rng = np.random.default_rng(21)
+    kind, q0, q1, w = [], [], [], []
+    for q in range(n):
+        kind.append(2), q0.append(q), q1.append(q), w.append(float(rng.choice([0.5, -1.0, 0.25])))
+    for i in range(n):
+        for j in range(i + 1, n):
+            kind.append(3), q0.append(i), q1.append(j), w.append(float(rng.choice([1.0, -0.5, 2.0, 0.75])))
+    axes = rng.integers(0, 3, (L, n))
+    angles = rng.uniform(0, 2 * np.pi, (L, n))
+    E0, g0 = O.mcclean_grad(n, axes, angles, O.Terms(kind, q0, q1, w))
+    c = _mc(n, L, axes, angles, kind, q0, q1, w, dtype=dtype)
+    for t in tiles:
+        c.set_tuning(t, 0, 0)
+        E, g = c.grad_run()
+        assert abs(E - E0) <= tol * max(1.0, abs(E0)), (t, E, E0)
+        assert rel_err(g, g0) <= tol, (t, rel_err(g, g0))
+        assert abs(c.run_expec_val() - E0) <= tol * max(1.0, abs(E0))
