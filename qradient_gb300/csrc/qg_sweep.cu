@@ -1097,8 +1097,8 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       // nothing diagonal to apply and no psi to write: a plain copy-out
       C* lout = p.lam_out + bd;
       for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = tl[stid + k * NTHREADS];
-    } else if (sizeof(R) == 4 && active && !UNCOMPUTE && d.has_diag && d.cost == COST_NONE && d.nz > 0) {
-      // complex64, the merged Z table alone: no per-element case tests
+    } else if (active && !UNCOMPUTE && d.has_diag && d.cost == COST_NONE && d.nz > 0) {
+      // the merged Z table alone: no per-element case tests
       C* lout = p.lam_out + bd;
       for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = cmul(tl[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
     } else if (active) {
