@@ -684,6 +684,89 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
   red_add3<R, G>(S, RS_XY + g0, acc);
 }
 
+// The last gate group of a backward sweep: its gradient reductions and its
+// inverse rotations in one pass (each task reads its amplitudes once,
+// reduces, rotates lambda -- and psi when PSI -- and writes them back).  The
+// reductions of the sweep's other groups must have been taken before: every
+// reduction sees lambda and psi before any inverse rotation.
+template <typename C, typename R, int G, bool PSI>
+__device__ __forceinline__ void redrot_group(C* tl, C* tp, int tsize, const SweepDesc& d, SetupShared& S, int g0) {
+  int b[G], ax[G], fm[G];
+  R uu[G], acc[G];
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    b[i] = d.xy[g0 + i].lbit;
+    ax[i] = d.xy[g0 + i].axis;
+    fm[i] = S.form[g0 + i];
+    uu[i] = sizeof(R) == 4 ? (R)S.uf[g0 + i] : (R)S.u[g0 + i];
+    acc[i] = (R)0;
+  }
+  int sbit[sizeof(R) == 4 ? G : 1];
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int i = 0; i < G; ++i) sbit[i] = sw<R>(1 << b[i]);
+  }
+  const int ntask = tsize >> G;
+  for (int tk = threadIdx.x; tk < ntask; tk += NTHREADS) {
+    int base = tk;
+#pragma unroll
+    for (int i = 0; i < G; ++i) base = insert0(base, b[i]);
+    int idx[1 << G];
+    if constexpr (sizeof(R) == 4) {
+      const int sb = sw<R>(base);
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) {
+        int x = sb;
+#pragma unroll
+        for (int i = 0; i < G; ++i)
+          if ((c >> i) & 1) x ^= sbit[i];
+        idx[c] = x;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) {
+        int x = base;
+#pragma unroll
+        for (int i = 0; i < G; ++i)
+          if ((c >> i) & 1) x |= 1 << b[i];
+        idx[c] = sw<R>(x);
+      }
+    }
+    C la[1 << G], qa[1 << G];
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) {
+      la[c] = tl[idx[c]];
+      qa[c] = tp[idx[c]];
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      // warp-uniform branch around the whole unrolled block
+      if (ax[i] == AX_X) {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] = red_pair_t<AX_X, C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], acc[i]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < (1 << G); ++c)
+          if (!((c >> i) & 1)) acc[i] = red_pair_t<AX_Y, C, R>(la[c], la[c | (1 << i)], qa[c], qa[c | (1 << i)], acc[i]);
+      }
+    }
+    rot_block_any<-1, 0, G>(la, ax[0], fm[0], uu[0]);
+    if (G > 1) rot_block_any<-1, (G > 1 ? 1 : 0), G>(la, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
+    if (G > 2) rot_block_any<-1, (G > 2 ? 2 : 0), G>(la, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
+#pragma unroll
+    for (int c = 0; c < (1 << G); ++c) tl[idx[c]] = la[c];
+    if (PSI) {
+      rot_block_any<-1, 0, G>(qa, ax[0], fm[0], uu[0]);
+      if (G > 1) rot_block_any<-1, (G > 1 ? 1 : 0), G>(qa, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
+      if (G > 2) rot_block_any<-1, (G > 2 ? 2 : 0), G>(qa, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
+#pragma unroll
+      for (int c = 0; c < (1 << G); ++c) tp[idx[c]] = qa[c];
+    }
+  }
+  red_add3<R, G>(S, RS_XY + g0, acc);
+}
+
 template <typename C, typename R, int SG>
 __device__ __forceinline__ void apply_all(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S) {
   for (int g0 = 0; g0 < d.nxy; g0 += 3) {
@@ -1080,19 +1163,27 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     }
     if (d.gslot >= 0) red_add<R>(S, RS_G, tG);
     __syncthreads();
-    // gradient reductions for the X/Y rotations (read-only pass)
-    for (int g0 = 0; g0 < d.nxy; g0 += 3) {
-      const int g = d.nxy - g0 < 3 ? d.nxy - g0 : 3;
+    // gradient reductions for the X/Y rotations of every group but the last
+    // (read-only), then the last group's reductions and inverse rotations in
+    // one pass, then the other groups' inverse rotations (they commute, so
+    // the group order is free)
+    const int glast = d.nxy > 0 ? ((d.nxy - 1) / 3) * 3 : 0;
+    for (int g0 = 0; g0 < glast; g0 += 3) reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+    if (d.nxy > 0) {
+      if (glast > 0) __syncthreads();  // the fused pass rewrites what the reductions above read
+      const int g = d.nxy - glast;
       if (g == 3)
-        reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+        redrot_group<C, R, 3, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
       else if (g == 2)
-        reduce_group<C, R, 2>(tl, tp, tsize, d, S, g0);
+        redrot_group<C, R, 2, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
       else
-        reduce_group<C, R, 1>(tl, tp, tsize, d, S, g0);
+        redrot_group<C, R, 1, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
+      __syncthreads();
     }
-    __syncthreads();
-    // inverse rotations (they commute, so the group order is free)
-    apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
+    for (int g0 = 0; g0 < glast; g0 += 3) {
+      apply_group<C, R, 3, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S, g0);
+      __syncthreads();
+    }
     if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
       // nothing diagonal to apply and no psi to write: a plain copy-out
       C* lout = p.lam_out + bd;
