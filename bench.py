@@ -492,7 +492,6 @@ def main():
     idx = phys.split(",")[local] if phys else str(local)
     clocks = ClockSampler(idx)
     clocks.start()
-    lib.qg_profile_enable(1)
     stream = torch.cuda.current_stream(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -507,6 +506,17 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
+    # per-kernel durations from a second pass of the same steps with an event
+    # pair around every launch (kept out of the timed region above: the
+    # events cost a little per launch)
+    lib.qg_profile_enable(1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_prof = e0.elapsed_time(e1)
     kinfo = {}
     for cls, name in ((0, "forward_sweep"), (1, "backward_sweep"), (2, "observable")):
         tot = ctypes.c_double(0.0)
@@ -579,13 +589,13 @@ def main():
                         "frac": achieved_gbs / hbm_peak if achieved_gbs else None,
                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
                 "launch_ms_avg": bwd_avg_s * 1e3, "launches": bwd_n,
-                "kernel_share": {k: v[0] / ms for k, v in kinfo.items()}}
+                "kernel_share": {k: v[0] / ms_prof for k, v in kinfo.items()}}
     else:
         roof = {"bound": "hbm", "kernel": "sweep_bwd_kernel<float,history>", "achieved": achieved_gbs,
                 "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak if achieved_gbs else None,
                 "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
                 "launch_ms_avg": bwd_avg_s * 1e3, "launches": bwd_n,
-                "kernel_share": {k: v[0] / ms for k, v in kinfo.items()}}
+                "kernel_share": {k: v[0] / ms_prof for k, v in kinfo.items()}}
 
     launches_per_step = (fwd_n + bwd_n + kinfo["observable"][1]) / args.steps + 1  # + the finalize kernel
     line = {
