@@ -582,6 +582,7 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
       rot_block_any<SG, 0, G>(el, ax[0], fm[0], uu[0]);
       if (G > 1) rot_block_any<SG, (G > 1 ? 1 : 0), G>(el, ax[G > 1 ? 1 : 0], fm[G > 1 ? 1 : 0], uu[G > 1 ? 1 : 0]);
       if (G > 2) rot_block_any<SG, (G > 2 ? 2 : 0), G>(el, ax[G > 2 ? 2 : 0], fm[G > 2 ? 2 : 0], uu[G > 2 ? 2 : 0]);
+      if (G > 3) rot_block_any<SG, (G > 3 ? 3 : 0), G>(el, ax[G > 3 ? 3 : 0], fm[G > 3 ? 3 : 0], uu[G > 3 ? 3 : 0]);
 #pragma unroll
       for (int c = 0; c < (1 << G); ++c) w[idx[c]] = el[c];
     }
@@ -765,6 +766,24 @@ __device__ __forceinline__ void redrot_group(C* tl, C* tp, int tsize, const Swee
     }
   }
   red_add3<R, G>(S, RS_XY + g0, acc);
+}
+
+// complex64 forward sweeps: groups of four rotations (16 amplitudes per
+// task in registers), one shared-memory round trip fewer per 12 rotations
+template <typename C, typename R>
+__device__ __forceinline__ void apply_all4(C* v, int tsize, const SweepDesc& d, const SetupShared& S) {
+  for (int g0 = 0; g0 < d.nxy; g0 += 4) {
+    const int g = d.nxy - g0 < 4 ? d.nxy - g0 : 4;
+    if (g == 4)
+      apply_group<C, R, 4, 1>(v, nullptr, tsize, d, S, g0);
+    else if (g == 3)
+      apply_group<C, R, 3, 1>(v, nullptr, tsize, d, S, g0);
+    else if (g == 2)
+      apply_group<C, R, 2, 1>(v, nullptr, tsize, d, S, g0);
+    else
+      apply_group<C, R, 1, 1>(v, nullptr, tsize, d, S, g0);
+    __syncthreads();
+  }
 }
 
 template <typename C, typename R, int SG>
@@ -973,7 +992,10 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
       }
     }
     __syncthreads();
-    apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
+    if constexpr (sizeof(R) == 4)
+      apply_all4<C, R>(tile, tsize, d, S);
+    else
+      apply_all<C, R, 1>(tile, nullptr, tsize, d, S);
     if (sizeof(R) == 4 && active && diag_store && d.cost == COST_NONE && d.nz > 0) {
       // complex64, the merged Z table alone: no per-element case tests
       C* out = p.psi_out + bd;
@@ -1167,9 +1189,26 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     // (read-only), then the last group's reductions and inverse rotations in
     // one pass, then the other groups' inverse rotations (they commute, so
     // the group order is free)
-    const int glast = d.nxy > 0 ? ((d.nxy - 1) / 3) * 3 : 0;
-    for (int g0 = 0; g0 < glast; g0 += 3) reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
-    if (d.nxy > 0) {
+    // (complex128 kernels other than the fixed-tile history one keep
+    // separate reduction and rotation passes: the fused pass's registers
+    // would spill there)
+    constexpr bool kFuse = sizeof(R) == 4 || (TB > 0 && !UNCOMPUTE);
+    if (!kFuse) {
+      for (int g0 = 0; g0 < d.nxy; g0 += 3) {
+        const int g = d.nxy - g0 < 3 ? d.nxy - g0 : 3;
+        if (g == 3)
+          reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+        else if (g == 2)
+          reduce_group<C, R, 2>(tl, tp, tsize, d, S, g0);
+        else
+          reduce_group<C, R, 1>(tl, tp, tsize, d, S, g0);
+      }
+      __syncthreads();
+    }
+    const int glast = !kFuse ? d.nxy : d.nxy > 0 ? ((d.nxy - 1) / 3) * 3 : 0;
+    if (kFuse)
+      for (int g0 = 0; g0 < glast; g0 += 3) reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+    if (kFuse && d.nxy > 0) {
       if (glast > 0) __syncthreads();  // the fused pass rewrites what the reductions above read
       const int g = d.nxy - glast;
       if (g == 3)
@@ -1180,9 +1219,13 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
         redrot_group<C, R, 1, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
       __syncthreads();
     }
-    for (int g0 = 0; g0 < glast; g0 += 3) {
-      apply_group<C, R, 3, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S, g0);
-      __syncthreads();
+    if (kFuse) {
+      for (int g0 = 0; g0 < glast; g0 += 3) {
+        apply_group<C, R, 3, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S, g0);
+        __syncthreads();
+      }
+    } else {
+      apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
     }
     if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
       // nothing diagonal to apply and no psi to write: a plain copy-out
