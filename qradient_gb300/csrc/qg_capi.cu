@@ -616,14 +616,18 @@ std::vector<ObsDesc> build_obs(const qg_circuit* c, const Program& P, bool grad,
 }
 
 template <typename R>
+// after_sweep: the previous launch in the stream is a sweep or observable
+// launch, so the first pass may start as its programmatic dependent.
 int run_observable(const std::vector<ObsDesc>& obs, const WsLayout& W, const typename C2T<R>::T* psi,
-                   typename C2T<R>::T* lam, char* ws, cudaStream_t st) {
+                   typename C2T<R>::T* lam, char* ws, cudaStream_t st, bool after_sweep) {
   double* partials = (double*)(ws + W.partials);
   const int32_t* ci = (const int32_t*)(ws + W.cost);
   const double* cd = (const double*)(ws + W.cost);
+  bool pdl = after_sweep;
   for (const ObsDesc& d : obs) {
     ProfScope ps(2, st);
-    QG_CUDA(launch_observable<R>(d, psi, lam, ci, cd, partials, W.G, W.G, st));
+    QG_CUDA(launch_observable<R>(d, psi, lam, ci, cd, partials, W.G, W.G, st, pdl));
+    pdl = true;
   }
   return QG_OK;
 }
@@ -656,7 +660,8 @@ int forward(const qg_circuit* c, const Program& P, const WsLayout& W, const doub
     p.psi_in = in;
     p.psi_out = out;
     ProfScope ps(0, st);
-    QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd_k[k], st, W.fwd_pipe));
+    // every sweep but the first follows a sweep launch: programmatic dependent
+    QG_CUDA(launch_sweep_fwd<R>(P.sweeps[k], p, W.grid_fwd_k[k], st, W.fwd_pipe, k > 0));
     in = out;
   }
   *final_state = in;
@@ -678,7 +683,7 @@ int do_run(const qg_circuit* c, const double* params, const void* ini, char* ws,
   const C* fin = nullptr;
   s = forward<R>(c, P, W, params, ini, false, ws, st, &fin);
   if (s) return s;
-  s = run_observable<R>(plan->obs, W, fin, nullptr, ws, st);
+  s = run_observable<R>(plan->obs, W, fin, nullptr, ws, st, !P.sweeps.empty());
   if (s) return s;
   QG_CUDA(launch_finalize((double*)(ws + W.partials), W.G, 0, c->n, 0, P.nslots, W.neslots, expec, nullptr, st));
   if (state_out) QG_CUDA(cudaMemcpyAsync(state_out, fin, W.state_bytes, cudaMemcpyDeviceToDevice, st));
@@ -714,11 +719,11 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
     // overwritten by the full-observable pass, which writes at least the
     // same slots, so E stays <psi|O|psi> (mc_clean.py:99-100)
     const std::vector<Term> one(1, c->terms[component]);
-    s = run_observable<R>(build_obs(c, P, true, true, &one), W, fin, lbuf[lc], ws, st);
+    s = run_observable<R>(build_obs(c, P, true, true, &one), W, fin, lbuf[lc], ws, st, !P.sweeps.empty());
     if (s) return s;
-    s = run_observable<R>(build_obs(c, P, false, false, nullptr), W, fin, nullptr, ws, st);
+    s = run_observable<R>(build_obs(c, P, false, false, nullptr), W, fin, nullptr, ws, st, true);
   } else {
-    s = run_observable<R>(plan->obs, W, fin, lbuf[lc], ws, st);
+    s = run_observable<R>(plan->obs, W, fin, lbuf[lc], ws, st, !P.sweeps.empty());
   }
   if (s) return s;
   SweepPtrs<R> p;
@@ -747,7 +752,8 @@ int do_grad(const qg_circuit* c, int op, const double* params, const void* ini, 
       p.psi_out = pbuf[pc];
     }
     ProfScope ps(1, st);
-    QG_CUDA(launch_sweep_bwd<R>(d, p, !history, W.grid_bwd_k[k], st));
+    // follows the observable pass or the previous backward sweep
+    QG_CUDA(launch_sweep_bwd<R>(d, p, !history, W.grid_bwd_k[k], st, true));
   }
   C* lam = lbuf[lc];
   if (c->kind == 1 && c->L > 0) {

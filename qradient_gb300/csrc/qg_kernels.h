@@ -14,17 +14,22 @@ int set_last_error(int status, const char* msg);
 template <typename R>
 int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe = false);
 
-// pipe: use the double-buffered forward kernel for sweeps that load their input
+// pipe: use the double-buffered forward kernel for sweeps that load their input.
+// pdl: launch as a programmatic dependent of the previous launch in the stream,
+// which must be a sweep or observable launch (their kernels trigger early and
+// wait for the previous grid before touching its outputs).
 template <typename R>
-cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe = false);
+cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe = false,
+                             bool pdl = false);
 
 template <typename R>
-cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st);
+cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st,
+                             bool pdl = false);
 
 template <typename R>
 cudaError_t launch_observable(const ObsDesc& d, const typename C2T<R>::T* psi, typename C2T<R>::T* lam,
                               const int32_t* cost_i, const double* cost_d, double* partials, int G, int grid,
-                              cudaStream_t st);
+                              cudaStream_t st, bool pdl = false);
 
 template <typename R>
 cudaError_t launch_cost_reduce(int n, const typename C2T<R>::T* lam, const typename C2T<R>::T* psi, int start_plus,

@@ -21,6 +21,34 @@ constexpr int kTileC64 = 12, kTileC128 = 11;
 template <typename R>
 constexpr int kTileFixed = sizeof(R) == 4 ? kTileC64 : kTileC128;
 
+// Programmatic dependent launch.  The sweep and observable kernels let the
+// next launch start at once (pdl_trigger) and, after their setup (which
+// reads only the angles and the descriptor), wait for the previous grid's
+// completion and memory (pdl_wait) before their first access to a state,
+// the cost tables or the partial sums.  Launched with the attribute after
+// one of these kernels, a kernel's CTAs take the SMs the previous grid's
+// finished CTAs free and run their setup while it drains.  Without the
+// attribute both instructions return at once.  The wait is the hardware's:
+// it ends when the previous grid has completed.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kern)(KArgs...), int grid, size_t smem, cudaStream_t st, bool pdl,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 // ---------------------------------------------------------------- helpers
 
 __device__ __forceinline__ double angle_of(const AngleRef& a, const double* params) {
@@ -814,6 +842,8 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   C* ctab = ztab + (1 << d.nz);
   __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
   sweep_setup<C, false>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
+  pdl_trigger();
+  pdl_wait();
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -914,6 +944,8 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
   C* ctab = ztab + (1 << d.nz);
   __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
   sweep_setup<C, false>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
+  pdl_trigger();
+  pdl_wait();
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -1049,6 +1081,8 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   C* ctab = ztab + (1 << d.nz);
   __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
   sweep_setup<C, true>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
+  pdl_trigger();
+  pdl_wait();
 
   const int tid = threadIdx.x;
   const LadderMasks lm = ladder_masks(n);
@@ -1387,6 +1421,8 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
     }
   }
   __syncthreads();
+  pdl_trigger();
+  pdl_wait();
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
@@ -1698,49 +1734,40 @@ template int sweep_ctas_per_sm<double>(const SweepDesc&, bool, bool, bool);
 template int sweep_ctas_per_sm<float>(const SweepDesc&, bool, bool, bool);
 
 template <typename R>
-cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe) {
+cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid, cudaStream_t st, bool pipe,
+                             bool pdl) {
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   if (pipe && d.start == START_LOAD) {
-    if (fixed_tile<R>(d)) {
-      sweep_fwd_pipe_kernel<R, kTileFixed<R>><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
-      return cudaGetLastError();
-    }
-    sweep_fwd_pipe_kernel<R, 0><<<grid, NTHREADS, sweep_smem<R>(d, false, true), st>>>(d, p);
-    return cudaGetLastError();
+    if (fixed_tile<R>(d))
+      return launch_pdl(sweep_fwd_pipe_kernel<R, kTileFixed<R>>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
+    return launch_pdl(sweep_fwd_pipe_kernel<R, 0>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
   }
-  sweep_fwd_kernel<R><<<grid, NTHREADS, sweep_smem<R>(d, false), st>>>(d, p);
-  return cudaGetLastError();
+  return launch_pdl(sweep_fwd_kernel<R>, grid, sweep_smem<R>(d, false), st, pdl, d, p);
 }
 
 template <typename R>
-cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st) {
+cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool uncompute, int grid, cudaStream_t st,
+                             bool pdl) {
   const size_t smem = sweep_smem<R>(d, true);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   if (fixed_tile<R>(d)) {
-    if (uncompute)
-      sweep_bwd_kernel<R, true, kTileFixed<R>><<<grid, NTHREADS, smem, st>>>(d, p);
-    else
-      sweep_bwd_kernel<R, false, kTileFixed<R>><<<grid, NTHREADS, smem, st>>>(d, p);
-    return cudaGetLastError();
+    if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, kTileFixed<R>>, grid, smem, st, pdl, d, p);
+    return launch_pdl(sweep_bwd_kernel<R, false, kTileFixed<R>>, grid, smem, st, pdl, d, p);
   }
-  if (uncompute)
-    sweep_bwd_kernel<R, true, 0><<<grid, NTHREADS, smem, st>>>(d, p);
-  else
-    sweep_bwd_kernel<R, false, 0><<<grid, NTHREADS, smem, st>>>(d, p);
-  return cudaGetLastError();
+  if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, 0>, grid, smem, st, pdl, d, p);
+  return launch_pdl(sweep_bwd_kernel<R, false, 0>, grid, smem, st, pdl, d, p);
 }
 
 template <typename R>
 cudaError_t launch_observable(const ObsDesc& d, const typename C2T<R>::T* psi, typename C2T<R>::T* lam,
                               const int32_t* cost_i, const double* cost_d, double* partials, int G, int grid,
-                              cudaStream_t st) {
+                              cudaStream_t st, bool pdl) {
   const size_t smem = ObsSmem<R>::bytes(d.t, d.ndiag);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
-  observable_kernel<R><<<grid, NTHREADS, smem, st>>>(d, psi, lam, cost_i, cost_d, partials, G);
-  return cudaGetLastError();
+  return launch_pdl(observable_kernel<R>, grid, smem, st, pdl, d, psi, lam, cost_i, cost_d, partials, G);
 }
 
 template <typename R>
@@ -1759,14 +1786,14 @@ cudaError_t launch_finalize(const double* partials, int G, int kind, int n, int 
   return cudaGetLastError();
 }
 
-template cudaError_t launch_sweep_fwd<double>(const SweepDesc&, const SweepPtrs<double>&, int, cudaStream_t, bool);
-template cudaError_t launch_sweep_fwd<float>(const SweepDesc&, const SweepPtrs<float>&, int, cudaStream_t, bool);
-template cudaError_t launch_sweep_bwd<double>(const SweepDesc&, const SweepPtrs<double>&, bool, int, cudaStream_t);
-template cudaError_t launch_sweep_bwd<float>(const SweepDesc&, const SweepPtrs<float>&, bool, int, cudaStream_t);
+template cudaError_t launch_sweep_fwd<double>(const SweepDesc&, const SweepPtrs<double>&, int, cudaStream_t, bool, bool);
+template cudaError_t launch_sweep_fwd<float>(const SweepDesc&, const SweepPtrs<float>&, int, cudaStream_t, bool, bool);
+template cudaError_t launch_sweep_bwd<double>(const SweepDesc&, const SweepPtrs<double>&, bool, int, cudaStream_t, bool);
+template cudaError_t launch_sweep_bwd<float>(const SweepDesc&, const SweepPtrs<float>&, bool, int, cudaStream_t, bool);
 template cudaError_t launch_observable<double>(const ObsDesc&, const double2*, double2*, const int32_t*, const double*,
-                                               double*, int, int, cudaStream_t);
+                                               double*, int, int, cudaStream_t, bool);
 template cudaError_t launch_observable<float>(const ObsDesc&, const float2*, float2*, const int32_t*, const double*,
-                                              double*, int, int, cudaStream_t);
+                                              double*, int, int, cudaStream_t, bool);
 template cudaError_t launch_cost_reduce<double>(int, const double2*, const double2*, int, int, double, const int32_t*,
                                                 const double*, double*, int, int, cudaStream_t);
 template cudaError_t launch_cost_reduce<float>(int, const float2*, const float2*, int, int, double, const int32_t*,
