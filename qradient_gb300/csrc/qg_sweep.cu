@@ -1123,37 +1123,66 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   // pointer plus offhi[k] (the parts are disjoint).
   TileBases tb(S.outside, n - t, n, d.bits, t);
   const int stid = sw<R>(tid);
+  // The copies of one element of a tile into this thread's slot k: undo the
+  // entangler that follows this sweep, (E^{-1} v)[y] = v[A y].  complex64
+  // takes the ladder image from its parts' images (fewer integer
+  // instructions), complex128 computes it (a shared-memory load costs more
+  // there than integer work).
+  auto lam_copy = [&](int k, uint64_t bd_, uint64_t lbase_) {
+    const int64_t oh = S.offhi[k];
+    if (d.lam_undo == ENT_CNOT) {
+      const uint64_t ax = sizeof(R) == 4 ? lbase_ ^ (uint64_t)ladk[k] : ladder_fwd(bd_ + (uint64_t)oh, lm);
+      cp_async_elem(&tl[stid + k * NTHREADS], p.lam_in + ax);
+    } else {
+      cp_async_elem(&tl[stid + k * NTHREADS], p.lam_in + bd_ + oh);
+    }
+  };
+  auto psi_copy = [&](int k, uint64_t bd_, uint64_t lbase_) {
+    const int64_t oh = S.offhi[k];
+    if (d.psi_undo == ENT_CNOT) {
+      const uint64_t ax = sizeof(R) == 4 ? lbase_ ^ (uint64_t)ladk[k] : ladder_fwd(bd_ + (uint64_t)oh, lm);
+      cp_async_elem(&tp[stid + k * NTHREADS], p.psi_in + ax);
+    } else {
+      cp_async_elem(&tp[stid + k * NTHREADS], p.psi_in + bd_ + oh);
+    }
+  };
+  // History mode reads psi and writes only lambda, so the next tile's copies
+  // go out early: psi's once the last pass that reads psi is done, each
+  // lambda element's as soon as this thread has stored it.  The DRAM round
+  // trip then overlaps the rest of the tile's work.  (Uncomputing writes
+  // psi back from its buffer: its tiles load at their start.)
+  constexpr bool kPrefetch = !UNCOMPUTE;
+  int64_t bnext = tb.advance();
+  if (kPrefetch && active && (int64_t)blockIdx.x < ntiles) {
+    const uint64_t bd0 = (uint64_t)(bnext | dep_lo);
+    const uint64_t lb0 = ladder_fwd((uint64_t)bnext, lm) ^ ldep;
+    for (int k = 0; k < nk; ++k) {
+      lam_copy(k, bd0, lb0);
+      psi_copy(k, bd0, lb0);
+    }
+  }
+  cp_async_commit();
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
-    const int64_t base = tb.advance();
+    const int64_t base = bnext;
+    bnext = tb.advance();
+    const bool more = tileid + gridDim.x < ntiles;
     const uint64_t bd = (uint64_t)(base | dep_lo);
+    const uint64_t bdn = (uint64_t)(bnext | dep_lo);
     const int zp = zpt | zpattern((uint64_t)base, d);
     const uint64_t lbase = ladder_fwd((uint64_t)base, lm) ^ ldep;
+    const uint64_t lbasen = kPrefetch && more ? ladder_fwd((uint64_t)bnext, lm) ^ ldep : 0;
     R tT = (R)0, tG = (R)0;
     if (active) {
-      // all of this thread's loads of the tile in flight at once (asynchronous
-      // global->shared copies), then one wait: a load-use loop would wait one
-      // memory round trip per element
-      const C* lin = p.lam_in + bd;
-      const C* pin = p.psi_in + bd;
-      if (sizeof(R) == 4 && d.lam_undo != ENT_CNOT && d.psi_undo != ENT_CNOT) {
+      // all of this thread's copies of the tile in flight at once
+      // (asynchronous global->shared), then one wait: a load-use loop would
+      // wait one memory round trip per element
+      if (!kPrefetch) {
         for (int k = 0; k < nk; ++k) {
-          const int64_t oh = S.offhi[k];
-          cp_async_elem(&tl[stid + k * NTHREADS], lin + oh);
-          cp_async_elem(&tp[stid + k * NTHREADS], pin + oh);
+          lam_copy(k, bd, lbase);
+          psi_copy(k, bd, lbase);
         }
-      } else {
-        for (int k = 0; k < nk; ++k) {
-          const int64_t oh = S.offhi[k];
-          // undo the entangler that follows this sweep: (E^{-1} v)[y] = v[A y];
-          // complex64 takes the image from its parts' images (fewer integer
-          // instructions), complex128 computes it (a shared-memory load costs
-          // more there than integer work)
-          const uint64_t ax = sizeof(R) == 4 ? lbase ^ (uint64_t)ladk[k] : ladder_fwd(bd + (uint64_t)oh, lm);
-          cp_async_elem(&tl[stid + k * NTHREADS], d.lam_undo == ENT_CNOT ? p.lam_in + ax : lin + oh);
-          cp_async_elem(&tp[stid + k * NTHREADS], d.psi_undo == ENT_CNOT ? p.psi_in + ax : pin + oh);
-        }
+        cp_async_commit();
       }
-      cp_async_commit();
       cp_async_wait<0>();
       const bool cz_l = d.lam_undo == ENT_CZ, cz_p = d.psi_undo == ENT_CZ;
       if (sizeof(R) == 4 && need_w && !cz_l && !cz_p && d.gslot < 0 && nk >= 4) {
@@ -1253,6 +1282,11 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
         redrot_group<C, R, 1, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
       __syncthreads();
     }
+    // psi is not read again in this tile (every pass above that reads it
+    // ended at a barrier): the next tile's psi copies go out now
+    if (kPrefetch && active && more) {
+      for (int k = 0; k < nk; ++k) psi_copy(k, bdn, lbasen);
+    }
     if (kFuse) {
       for (int g0 = 0; g0 < glast; g0 += 3) {
         apply_group<C, R, 3, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S, g0);
@@ -1261,14 +1295,23 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     } else {
       apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
     }
+    // (in history mode each stored element's slot takes the next tile's
+    // lambda copy at once: only this thread reads its slots here)
+    const bool pf = kPrefetch && more;
     if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
       // nothing diagonal to apply and no psi to write: a plain copy-out
       C* lout = p.lam_out + bd;
-      for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = tl[stid + k * NTHREADS];
+      for (int k = 0; k < nk; ++k) {
+        lout[S.offhi[k]] = tl[stid + k * NTHREADS];
+        if (pf) lam_copy(k, bdn, lbasen);
+      }
     } else if (active && !UNCOMPUTE && d.has_diag && d.cost == COST_NONE && d.nz > 0) {
       // the merged Z table alone: no per-element case tests
       C* lout = p.lam_out + bd;
-      for (int k = 0; k < nk; ++k) lout[S.offhi[k]] = cmul(tl[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
+      for (int k = 0; k < nk; ++k) {
+        lout[S.offhi[k]] = cmul(tl[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
+        if (pf) lam_copy(k, bdn, lbasen);
+      }
     } else if (active) {
       C* lout = p.lam_out + bd;
       C* pout = p.psi_out + bd;
@@ -1281,10 +1324,13 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
         if (UNCOMPUTE)
           pout[oh] = cscale(apply_diag<C>(tp[e], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true),
                             psi_mult);
+        if (pf) lam_copy(k, bdn, lbasen);
       }
     }
+    if (kPrefetch) cp_async_commit();
     __syncthreads();
   }
+  cp_async_wait<0>();
 
   // Z rotations: per-thread sums into the warp slots once per CTA
   if (d.nz > 0) {
