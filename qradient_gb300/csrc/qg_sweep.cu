@@ -1146,14 +1146,16 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       cp_async_elem(&tp[stid + k * NTHREADS], p.psi_in + bd_ + oh);
     }
   };
-  // History mode reads psi and writes only lambda, so the next tile's copies
-  // go out early: psi's once the last pass that reads psi is done, each
-  // lambda element's as soon as this thread has stored it.  The DRAM round
-  // trip then overlaps the rest of the tile's work.  (Uncomputing writes
-  // psi back from its buffer: its tiles load at their start.)
-  constexpr bool kPrefetch = !UNCOMPUTE;
+  // The next tile's copies go out early, so that their DRAM round trip
+  // overlaps the rest of this tile's work: each element's as soon as this
+  // thread has stored it (the store pass reads only the thread's own slots,
+  // after the last barrier of the cross-thread passes), and in history mode,
+  // where psi is only read, psi's already once the last pass that reads psi
+  // is done.  A tile's copies touch only that tile (its own elements, or
+  // their ladder images in the other buffer of a pair), which no other CTA
+  // writes.
   int64_t bnext = tb.advance();
-  if (kPrefetch && active && (int64_t)blockIdx.x < ntiles) {
+  if (active && (int64_t)blockIdx.x < ntiles) {
     const uint64_t bd0 = (uint64_t)(bnext | dep_lo);
     const uint64_t lb0 = ladder_fwd((uint64_t)bnext, lm) ^ ldep;
     for (int k = 0; k < nk; ++k) {
@@ -1169,20 +1171,12 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     const uint64_t bd = (uint64_t)(base | dep_lo);
     const uint64_t bdn = (uint64_t)(bnext | dep_lo);
     const int zp = zpt | zpattern((uint64_t)base, d);
-    const uint64_t lbase = ladder_fwd((uint64_t)base, lm) ^ ldep;
-    const uint64_t lbasen = kPrefetch && more ? ladder_fwd((uint64_t)bnext, lm) ^ ldep : 0;
+    const uint64_t lbasen = more ? ladder_fwd((uint64_t)bnext, lm) ^ ldep : 0;
     R tT = (R)0, tG = (R)0;
     if (active) {
-      // all of this thread's copies of the tile in flight at once
-      // (asynchronous global->shared), then one wait: a load-use loop would
-      // wait one memory round trip per element
-      if (!kPrefetch) {
-        for (int k = 0; k < nk; ++k) {
-          lam_copy(k, bd, lbase);
-          psi_copy(k, bd, lbase);
-        }
-        cp_async_commit();
-      }
+      // this thread's copies of the tile (issued during the previous tile, all
+      // in flight at once) have landed: a load-use loop would wait one
+      // memory round trip per element
       cp_async_wait<0>();
       const bool cz_l = d.lam_undo == ENT_CZ, cz_p = d.psi_undo == ENT_CZ;
       if (sizeof(R) == 4 && need_w && !cz_l && !cz_p && d.gslot < 0 && nk >= 4) {
@@ -1282,9 +1276,9 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
         redrot_group<C, R, 1, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
       __syncthreads();
     }
-    // psi is not read again in this tile (every pass above that reads it
-    // ended at a barrier): the next tile's psi copies go out now
-    if (kPrefetch && active && more) {
+    // history mode: psi is not read again in this tile (every pass above
+    // that reads it ended at a barrier): the next tile's psi copies go out now
+    if (!UNCOMPUTE && active && more) {
       for (int k = 0; k < nk; ++k) psi_copy(k, bdn, lbasen);
     }
     if (kFuse) {
@@ -1295,9 +1289,9 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     } else {
       apply_all<C, R, -1>(tl, UNCOMPUTE ? tp : nullptr, tsize, d, S);
     }
-    // (in history mode each stored element's slot takes the next tile's
-    // lambda copy at once: only this thread reads its slots here)
-    const bool pf = kPrefetch && more;
+    // (each stored element's slots take the next tile's copies at once: only
+    // this thread reads its slots here)
+    const bool pf = more;
     if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
       // nothing diagonal to apply and no psi to write: a plain copy-out
       C* lout = p.lam_out + bd;
@@ -1325,9 +1319,10 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
           pout[oh] = cscale(apply_diag<C>(tp[e], x, zpe, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, true),
                             psi_mult);
         if (pf) lam_copy(k, bdn, lbasen);
+        if (pf && UNCOMPUTE) psi_copy(k, bdn, lbasen);
       }
     }
-    if (kPrefetch) cp_async_commit();
+    cp_async_commit();
     __syncthreads();
   }
   cp_async_wait<0>();
