@@ -976,10 +976,11 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
   auto issue = [&](int64_t base, C* dst) {
     if (active) {
       const uint64_t bd = (uint64_t)(base | dep_lo);
-      // complex64 (issue-bound) has a loop per case and takes the ladder
-      // image from its parts' images; complex128 (FP64-bound) one loop that
-      // computes the image (a shared-memory load costs more there than
-      // integer work)
+      // complex64, limited by its integer and shared-memory instructions,
+      // has a loop per case and takes the ladder image from its parts'
+      // images; complex128, bound by the FP64 pipe, has one loop that
+      // computes the image (measured: a shared-memory load cost more there
+      // than the integer work)
       if constexpr (sizeof(R) == 4) {
         if (d.pre == ENT_CNOT) {
           const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
