@@ -160,55 +160,10 @@ __device__ __forceinline__ double rot_form(double theta, int* form, double* kapp
 }
 
 // Apply one X/Y rotation (scaled form) to the pair (a, b) = (bit 0, bit 1).
-// SG = +1 applies R(theta), SG = -1 applies R(-theta); a compile-time sign,
-// so it folds into the FMAs' operand negations.
-template <int SG, typename C, typename R>
-__device__ __forceinline__ void rot_pair(C& a, C& b, int axis, int form, R u) {
-  const C a0 = a, b0 = b;
-  if (axis == AX_X) {
-    // -i * SG applied to the partner: (-i v) = (v.y, -v.x)
-    if (form == 0) {
-      const R us = SG > 0 ? u : -u;
-      a.x = fma(us, b0.y, a0.x);
-      a.y = fma(-us, b0.x, a0.y);
-      b.x = fma(us, a0.y, b0.x);
-      b.y = fma(-us, a0.x, b0.y);
-    } else if (SG > 0) {
-      a.x = fma(u, a0.x, b0.y);
-      a.y = fma(u, a0.y, -b0.x);
-      b.x = fma(u, b0.x, a0.y);
-      b.y = fma(u, b0.y, -a0.x);
-    } else {
-      a.x = fma(u, a0.x, -b0.y);
-      a.y = fma(u, a0.y, b0.x);
-      b.x = fma(u, b0.x, -a0.y);
-      b.y = fma(u, b0.y, a0.x);
-    }
-  } else {
-    // Y: [[1, -t],[t, 1]] (form 0) or [[u, -1],[1, u]] (form 1)
-    if (form == 0) {
-      const R us = SG > 0 ? u : -u;
-      a.x = fma(-us, b0.x, a0.x);
-      a.y = fma(-us, b0.y, a0.y);
-      b.x = fma(us, a0.x, b0.x);
-      b.y = fma(us, a0.y, b0.y);
-    } else if (SG > 0) {
-      a.x = fma(u, a0.x, -b0.x);
-      a.y = fma(u, a0.y, -b0.y);
-      b.x = fma(u, b0.x, a0.x);
-      b.y = fma(u, b0.y, a0.y);
-    } else {
-      a.x = fma(u, a0.x, b0.x);
-      a.y = fma(u, a0.y, b0.y);
-      b.x = fma(u, b0.x, -a0.x);
-      b.y = fma(u, b0.y, -a0.y);
-    }
-  }
-}
-
-// The same rotation with axis and form fixed at compile time (for unrolled
-// register code, where a runtime branch would be if-converted and all four
-// variants issued under predication).
+// SG = +1 applies R(theta), SG = -1 applies R(-theta): a compile-time sign,
+// folded into the FMAs' operand negations.  Axis and form are compile-time
+// too: in unrolled register code a runtime branch would be if-converted and
+// all four variants issued under predication.
 template <int SG, int AXIS, int FORM, typename C, typename R>
 __device__ __forceinline__ void rot_pair_t(C& a, C& b, R u) {
   const C a0 = a, b0 = b;
@@ -619,22 +574,6 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
 
 // Im<lam|P|psi> pair term: X: Im(conj la qb) + Im(conj lb qa);
 // Y: -Re(conj la qb) + Re(conj lb qa)
-template <typename C, typename R>
-__device__ __forceinline__ R red_pair(const C& la, const C& lb, const C& qa, const C& qb, int axis, R a) {
-  if (axis == AX_X) {
-    a = fma(la.x, qb.y, a);
-    a = fma(-la.y, qb.x, a);
-    a = fma(lb.x, qa.y, a);
-    a = fma(-lb.y, qa.x, a);
-  } else {
-    a = fma(-la.x, qb.x, a);
-    a = fma(-la.y, qb.y, a);
-    a = fma(lb.x, qa.x, a);
-    a = fma(lb.y, qa.y, a);
-  }
-  return a;
-}
-
 template <int AXIS, typename C, typename R>
 __device__ __forceinline__ R red_pair_t(const C& la, const C& lb, const C& qa, const C& qb, R a) {
   if (AXIS == AX_X) {
