@@ -27,7 +27,10 @@
  *     caller's workspace, sized by qg_workspace_size.
  *   - Calls are ordered on the given stream; a circuit handle is immutable
  *     after creation and may be used from several threads on distinct streams
- *     and workspaces.
+ *     and workspaces.  Inside one call, each sweep launch after the first is
+ *     a programmatic dependent of the previous one (its setup overlaps that
+ *     sweep's tail; it touches no state before that sweep completes); the
+ *     call's first launch is ordered after earlier work as usual.
  *   - Errors are returned as status codes (never traps); qg_last_error()
  *     gives a message for the calling thread.
  */
