@@ -115,13 +115,27 @@ bool fwd_pipelined(const qg_circuit* c, int dtype) {
   return env_int(dtype == QG_C128 ? "QG_FWD_PIPE_C128" : "QG_FWD_PIPE_C64", 1) != 0;
 }
 
-int default_tile_bits(int dtype) {
-  return dtype == QG_C128 ? env_int("QG_TILE_BITS_C128", 11) : env_int("QG_TILE_BITS_C64", 12);
+// Sweeps per layer of a layout with t tile bits, c of them kept low in the
+// high-bit sweeps for coalescing.
+int sweeps_per_layer(int n, int t, int c) { return n <= t ? 1 : 1 + (n - t + (t - c) - 1) / (t - c); }
+
+// Default tile bits: 11 (complex128) / 12 (complex64), the fastest at
+// n = 24.  complex128 takes 12 where that saves a sweep per layer (n = 20,
+// 21, 28-30): measured 1.032 -> 1.353 circuits/s at n = 28, L = 10 (4 -> 3
+// sweeps) and 68.6 -> 69.6 at n = 20, L = 50 (3 -> 2).
+int default_tile_bits(int dtype, int n) {
+  if (dtype == QG_C128) {
+    const int t = env_int("QG_TILE_BITS_C128", 0);
+    if (t > 0) return t;
+    // (from n = 20 on, where a state spans hundreds of tiles either way)
+    return n >= 20 && sweeps_per_layer(n, 12, 3) < sweeps_per_layer(n, 11, 3) ? 12 : 11;
+  }
+  return env_int("QG_TILE_BITS_C64", 12);
 }
 
 Layout make_layout(int n, int dtype, int tile_bits) {
   Layout lay;
-  int t = tile_bits > 0 ? tile_bits : default_tile_bits(dtype);
+  int t = tile_bits > 0 ? tile_bits : default_tile_bits(dtype, n);
   const int c = dtype == QG_C128 ? 3 : 4;
   t = std::max(c + 2, std::min(t, max_tile_bits(dtype)));
   if (n <= t) {

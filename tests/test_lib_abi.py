@@ -132,6 +132,23 @@ def test_optimiser_steps_and_component_gradient_validate_arguments():
     lib.qg_destroy(h)
 
 
+def test_default_tile_bits_save_sweeps():
+    """complex128 takes 12-bit tiles where they need one sweep per layer
+    fewer than 11-bit ones (n = 20, 21, 28-30), else 11; complex64 12."""
+    from qradient_gb300 import _lib
+
+    lib = _lib.load()
+    t, c, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    for n, want128 in ((16, 11), (19, 11), (20, 12), (21, 12), (24, 11), (27, 11), (28, 12), (30, 12), (31, 11)):
+        st, h = _create(n, 1, np.zeros((1, n)))
+        assert st == 0
+        assert lib.qg_get_tuning(h, 0, ctypes.byref(t), ctypes.byref(c), ctypes.byref(f)) == 0
+        assert t.value == want128, n
+        assert lib.qg_get_tuning(h, 1, ctypes.byref(t), ctypes.byref(c), ctypes.byref(f)) == 0
+        assert t.value == 12, n
+        lib.qg_destroy(h)
+
+
 def test_tuning_knobs_validate_and_report():
     from qradient_gb300 import _lib
 
@@ -148,10 +165,11 @@ def test_tuning_knobs_validate_and_report():
     assert lib.qg_set_tuning(h, 0, 11, 0, 3) == INV
     assert lib.qg_set_tuning(h, 0, 11, 0, 4) == INV
     t, c, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    for bits, flags in ((10, 1), (12, 2), (0, 0)):
+    for bits, flags in ((10, 1), (11, 2), (0, 0)):
         assert lib.qg_set_tuning(h, 0, bits, 0, flags) == 0
         assert lib.qg_get_tuning(h, 0, ctypes.byref(t), ctypes.byref(c), ctypes.byref(f)) == 0
-        assert t.value == (bits or 11)
+        # default at n = 20: 12 bits, two sweeps per layer where 11 needs three
+        assert t.value == (bits or 12)
         assert f.value in (1, 2) and (flags == 0 or f.value == flags)
     # history workspace holds one state per sweep: deeper fusion, fewer sweeps
     sizes = []
