@@ -844,9 +844,10 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
 // in flight while the current tile is computed: each CTA owns two tile
 // buffers; the loads of tile i+1 are issued as asynchronous global->shared
 // copies (cp.async, one amplitude each, gathered through the CNOT ladder
-// where the sweep starts with it) before tile i's gates run.  The diagonal
-// and the CZ sign, which the plain kernel applies on load, run as a pass
-// over each thread's own landed elements.
+// where the sweep starts with it) before tile i's gates run.  The cost phase
+// and the CZ sign, which the plain kernel applies on load, run as a pass over
+// each thread's own landed elements; a diagonal that commutes with the
+// sweep's rotations is applied as the tile is stored.
 
 __device__ __forceinline__ void cp_async_elem(void* dst_smem, const double2* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
