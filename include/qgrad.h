@@ -253,15 +253,18 @@ int qg_batch_launch(int dtype, const qg_batch_job* jobs_dev, int njobs, int max_
 
 /* ---- Allocation-free gradient (no counterpart in the reference).
  * For callers that cannot allocate device memory where they need a
- * gradient (inside a CUDA-graph capture, under a host that owns every
- * device allocation, in a loop that forbids allocation after start-up).
- * Same inputs and outputs as qg_grad in uncompute mode, but the scratch is a
- * library-owned static device array of QG_NOALLOC_SCRATCH_BYTES that every
- * GPU loading the library holds until exit.  Circuits whose uncompute
+ * gradient: plug-ins whose host process owns every device allocation
+ * through its own pool, and real-time loops that forbid allocation (which
+ * may synchronise the device) after start-up.  Same inputs and outputs as
+ * qg_grad in uncompute mode, but the scratch is a library-owned static
+ * device array of QG_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library's device code holds until exit.  Circuits whose uncompute
  * workspace exceeds it get QG_ERR_UNSUPPORTED.  The first call on a device
- * looks up the array's address; make it before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race, so order them (one
- * stream). */
+ * looks up the array's address (with that device current) and caches it; a
+ * context reset (cudaDeviceReset) invalidates the cached address, so the
+ * entry point must not be used after one.  Calls share the array and it
+ * keeps the previous call's contents: calls that overlap on the GPU race,
+ * so order them (one stream). */
 #define QG_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
 int qg_grad_noalloc(const qg_circuit* c, int dtype, const double* params_dev, const void* ini_state_dev,
                     double* expec_dev, double* grad_dev, qg_stream stream);

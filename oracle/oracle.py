@@ -49,8 +49,10 @@ def lib():
         for name, args in {
             "qgo_mcclean_run": [I, I, P, P, I, I, I, P, P, P, P, P, P, P],
             "qgo_mcclean_grad": [I, I, P, P, I, I, I, P, P, P, P, P, P, P],
+            "qgo_mcclean_grad_uncompute": [I, I, P, P, I, I, I, P, P, P, P, P, P, P],
             "qgo_qaoa_run": [I, I, P, P, I, P, P, P, P, P, P, P],
             "qgo_qaoa_grad": [I, I, P, P, I, P, P, P, P, P, P, P],
+            "qgo_qaoa_grad_uncompute": [I, I, P, P, I, P, P, P, P, P, P, P],
             "qgo_maxcut_table": [I, I, P, P],
             "qgo_entangle": [I, I, I, P],
             "qgo_num_threads": [],
@@ -105,15 +107,18 @@ def _chk(st):
         raise ValueError("oracle status %d" % st)
 
 
-def mcclean_grad(n, axes, angles, terms, entangler=ENT_CNOT, placement=PLACE_BEFORE, ini=None):
+def mcclean_grad(n, axes, angles, terms, entangler=ENT_CNOT, placement=PLACE_BEFORE, ini=None, uncompute=False):
+    """McClean.grad_run; uncompute=True keeps one psi instead of the L+1
+    stored states (for sizes whose history does not fit in host memory)."""
     axes = _c(axes, np.int32)
     angles = _c(angles, np.float64)
     L = axes.shape[0]
     ini = _c(ini, np.complex128)
     E = np.zeros(1)
     g = np.zeros((L, n))
-    _chk(lib().qgo_mcclean_grad(n, L, _p(axes), _p(angles), entangler, placement, len(terms), _p(terms.kind),
-                                _p(terms.q0), _p(terms.q1), _p(terms.w), _p(ini), _p(E), _p(g)))
+    f = lib().qgo_mcclean_grad_uncompute if uncompute else lib().qgo_mcclean_grad
+    _chk(f(n, L, _p(axes), _p(angles), entangler, placement, len(terms), _p(terms.kind), _p(terms.q0),
+           _p(terms.q1), _p(terms.w), _p(ini), _p(E), _p(g)))
     return float(E[0]), g
 
 
@@ -129,15 +134,17 @@ def mcclean_run(n, axes, angles, terms, entangler=ENT_CNOT, placement=PLACE_BEFO
     return (float(E[0]), st) if want_state else float(E[0])
 
 
-def qaoa_grad(n, betas, gammas, terms, ini=None):
+def qaoa_grad(n, betas, gammas, terms, ini=None, uncompute=False):
+    """Qaoa.grad_run; uncompute=True keeps one psi instead of 2p+1 states."""
     betas = _c(betas, np.float64)
     gammas = _c(gammas, np.float64)
     p = betas.shape[0]
     ini = _c(ini, np.complex128)
     E = np.zeros(1)
     g = np.zeros((p, 2))
-    _chk(lib().qgo_qaoa_grad(n, p, _p(betas), _p(gammas), len(terms), _p(terms.kind), _p(terms.q0), _p(terms.q1),
-                             _p(terms.w), _p(ini), _p(E), _p(g)))
+    f = lib().qgo_qaoa_grad_uncompute if uncompute else lib().qgo_qaoa_grad
+    _chk(f(n, p, _p(betas), _p(gammas), len(terms), _p(terms.kind), _p(terms.q0), _p(terms.q1), _p(terms.w),
+           _p(ini), _p(E), _p(g)))
     return float(E[0]), g
 
 

@@ -20,8 +20,11 @@
  *   - qradient/circuit_logic/base.py:17-20 expec_val
  *   - qradient/circuit_logic/mc_clean.py:27-78 run_expec_val / grad_run
  *   - qradient/circuit_logic/qaoa.py:23-70 run_expec_val / grad_run
- * with the same history-storing adjoint sweep (L+1 stored states, one
- * rot + drot pass per parameter), parallelised over amplitudes with OpenMP.
+ * with the same history-storing adjoint sweep (L+1 stored states; per
+ * parameter the rot + drot of the reference applied per amplitude and summed
+ * against the stored state in one pass), parallelised over amplitudes with
+ * OpenMP.  An uncompute mode (psi taken backwards instead of stored) serves
+ * the sizes whose L+1 host states do not fit.
  *
  * Index convention: qubit q is bit (n-1-q) of the basis index
  * (kron(id(2^q), op, id(2^(n-q-1))), state.py:84-88).  States are
@@ -250,54 +253,128 @@ int qgo_mcclean_run(int n, int L, const int* axes, const double* angles, int ent
   return QGO_OK;
 }
 
+/* One gradient entry of McClean.grad_run (mc_clean.py:72-75): the
+ * reference applies __rot(i, q) and __drot(i, q, -1) to a copy of lambda
+ * and takes -2 Re <hist|copy>.  Here the same two gate updates run per
+ * amplitude pair (X/Y, state.py:90-97, 142-149) or per amplitude (Z,
+ * state.py:168-175) in registers, each element receiving exactly the
+ * operations of the two full-vector passes, and the products with conj(hist)
+ * are summed in the same pass: no copy of lambda and no write. */
+static double grad_entry(const cplx* h, const cplx* v, int n, int q, int axis, double angle) {
+  double s = 0;
+  if (axis == QGO_Z) {
+    const cplx r0 = cexp(-0.5 * I * angle), r1 = cexp(0.5 * I * angle);  /* zrot(angle) */
+    const cplx d0 = -0.5 * I * cexp(-0.5 * I * -angle), d1 = 0.5 * I * cexp(0.5 * I * -angle);  /* dzrot(-angle) */
+    const int64_t N = (int64_t)1 << n;
+    const int64_t bp = bitpos(n, q);
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int64_t x = 0; x < N; x++) {
+      const int one = (int)((x >> bp) & 1);
+      const cplx r = v[x] * (one ? r1 : r0);
+      const cplx d = r * (one ? d1 : d0);
+      s += creal(conj(h[x]) * d);
+    }
+    return -2.0 * s;
+  }
+  const double rs = sin(0.5 * angle), rc = cos(0.5 * angle);       /* rot(angle) */
+  const double ds = sin(0.5 * -angle), dc = cos(0.5 * -angle);     /* drot(-angle) */
+  const int64_t half = (int64_t)1 << (n - 1);
+  const int64_t stride = (int64_t)1 << bitpos(n, q);
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (int64_t k = 0; k < half; k++) {
+    const int64_t a = ((k & ~(stride - 1)) << 1) | (k & (stride - 1));
+    const int64_t b = a | stride;
+    const cplx va = v[a], vb = v[b];
+    cplx pa, pb;
+    if (axis == QGO_X) {
+      pa = -I * vb;
+      pb = -I * va;
+    } else {
+      pa = -vb;
+      pb = va;
+    }
+    const cplx ra = rs * pa + rc * va, rb = rs * pb + rc * vb;
+    if (axis == QGO_X) {
+      pa = -I * rb;
+      pb = -I * ra;
+    } else {
+      pa = -rb;
+      pb = ra;
+    }
+    const cplx da = 0.5 * dc * pa - 0.5 * ds * ra, db = 0.5 * dc * pb - 0.5 * ds * rb;
+    s += creal(conj(h[a]) * da) + creal(conj(h[b]) * db);
+  }
+  return -2.0 * s;
+}
+
 /* McClean.grad_run (mc_clean.py:47-78).  Forward: store the state before
  * each layer's rotations; E = Re <psi|O psi>.  Backward, per layer: undo the
- * rotations on lambda, then for every qubit rot + drot(-theta) on a copy and
- * grad = -2 Re <hist|copy>. */
-int qgo_mcclean_grad(int n, int L, const int* axes, const double* angles, int entangler, int placement, int nterms,
-                     const int* kind, const int* q0, const int* q1, const double* w, const double* ini, double* E,
-                     double* grad) {
+ * rotations on lambda, then for every qubit grad = -2 Re <hist|drot rot lam>
+ * (grad_entry), then the inverse ladder.
+ * mode 0 keeps the reference's history of L+1 states (mc_clean.py:22,60);
+ * mode 1 (for sizes where L+1 host states do not fit) keeps one psi and
+ * uncomputes it alongside lambda: the inverse rotations and inverse ladder
+ * take psi back to the state the history would hold, up to rounding
+ * (about L n ulps). */
+static int mcclean_grad_impl(int n, int L, const int* axes, const double* angles, int entangler, int placement,
+                             int nterms, const int* kind, const int* q0, const int* q1, const double* w,
+                             const double* ini, double* E, double* grad, int uncompute) {
   int st = check_mcclean(n, L, axes);
   if (st) return st;
   const int64_t N = (int64_t)1 << n;
-  cplx* hist = (cplx*)malloc(sizeof(cplx) * (size_t)N * (size_t)(L + 1));
+  const size_t nh = uncompute ? 1 : (size_t)(L + 1);
+  cplx* hist = (cplx*)malloc(sizeof(cplx) * (size_t)N * nh);
   cplx* v = (cplx*)malloc(sizeof(cplx) * (size_t)N);
-  cplx* tmp = (cplx*)malloc(sizeof(cplx) * (size_t)N);
   cplx* scr = (cplx*)malloc(sizeof(cplx) * (size_t)N);
-  if (!hist || !v || !tmp || !scr) {
+  if (!hist || !v || !scr) {
     free(hist);
     free(v);
-    free(tmp);
     free(scr);
     return QGO_ENOMEM;
   }
+  cplx* psi = hist; /* uncompute mode: the one psi */
   mcclean_start(v, n, ini);
   for (int i = 0; i < L; i++) {
     if (placement == 0) entangle(v, scr, n, entangler, 0);
-    memcpy(hist + (size_t)i * N, v, sizeof(cplx) * (size_t)N);
+    if (!uncompute) memcpy(hist + (size_t)i * N, v, sizeof(cplx) * (size_t)N);
     for (int q = 0; q < n; q++) rot(v, n, q, axes[i * n + q], angles[i * n + q]);
     if (placement == 1) entangle(v, scr, n, entangler, 0);
   }
-  memcpy(hist + (size_t)L * N, v, sizeof(cplx) * (size_t)N);
-  apply_observable(hist + (size_t)L * N, v, n, nterms, kind, q0, q1, w);
-  *E = re_vdot(hist + (size_t)L * N, v, N);
+  cplx* last = uncompute ? psi : hist + (size_t)L * N;
+  memcpy(last, v, sizeof(cplx) * (size_t)N);
+  apply_observable(last, v, n, nterms, kind, q0, q1, w);
+  *E = re_vdot(last, v, N);
   for (int i = L - 1; i >= 0; i--) {
-    if (placement == 1) entangle(v, scr, n, entangler, 1);
-    for (int q = 0; q < n; q++) rot(v, n, q, axes[i * n + q], -angles[i * n + q]);
-    memcpy(tmp, v, sizeof(cplx) * (size_t)N);
-    for (int q = 0; q < n; q++) {
-      rot(v, n, q, axes[i * n + q], angles[i * n + q]);
-      drot(v, n, q, axes[i * n + q], -angles[i * n + q]);
-      grad[i * n + q] = -2.0 * re_vdot(hist + (size_t)i * N, v, N);
-      memcpy(v, tmp, sizeof(cplx) * (size_t)N);
+    if (placement == 1) {
+      entangle(v, scr, n, entangler, 1);
+      if (uncompute) entangle(psi, scr, n, entangler, 1);
     }
-    if (placement == 0) entangle(v, scr, n, entangler, 1);
+    for (int q = 0; q < n; q++) rot(v, n, q, axes[i * n + q], -angles[i * n + q]);
+    if (uncompute)
+      for (int q = 0; q < n; q++) rot(psi, n, q, axes[i * n + q], -angles[i * n + q]);
+    const cplx* h = uncompute ? psi : hist + (size_t)i * N;
+    for (int q = 0; q < n; q++) grad[i * n + q] = grad_entry(h, v, n, q, axes[i * n + q], angles[i * n + q]);
+    if (placement == 0) {
+      entangle(v, scr, n, entangler, 1);
+      if (uncompute) entangle(psi, scr, n, entangler, 1);
+    }
   }
   free(hist);
   free(v);
-  free(tmp);
   free(scr);
   return QGO_OK;
+}
+
+int qgo_mcclean_grad(int n, int L, const int* axes, const double* angles, int entangler, int placement, int nterms,
+                     const int* kind, const int* q0, const int* q1, const double* w, const double* ini, double* E,
+                     double* grad) {
+  return mcclean_grad_impl(n, L, axes, angles, entangler, placement, nterms, kind, q0, q1, w, ini, E, grad, 0);
+}
+
+int qgo_mcclean_grad_uncompute(int n, int L, const int* axes, const double* angles, int entangler, int placement,
+                               int nterms, const int* kind, const int* q0, const int* q1, const double* w,
+                               const double* ini, double* E, double* grad) {
+  return mcclean_grad_impl(n, L, axes, angles, entangler, placement, nterms, kind, q0, q1, w, ini, E, grad, 1);
 }
 
 /* Classical (diagonal) Hamiltonian from the z and zz terms
@@ -384,59 +461,86 @@ int qgo_qaoa_run(int n, int p, const double* betas, const double* gammas, int nt
   return QGO_OK;
 }
 
+/* grad[i, 0] of Qaoa.grad_run (qaoa.py:60-64): -2 Re <h| x_summed lam> with
+ * x_summed = 1/2 sum_q (-i X_q) (state.py:107-123), evaluated per amplitude
+ * and summed in the same pass (no copy of lambda). */
+static double grad_beta(const cplx* h, const cplx* v, int n) {
+  const int64_t N = (int64_t)1 << n;
+  double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (int64_t x = 0; x < N; x++) {
+    cplx acc = 0;
+    for (int q = 0; q < n; q++) acc += 0.5 * (-I) * v[x ^ ((int64_t)1 << bitpos(n, q))];
+    s += creal(conj(h[x]) * acc);
+  }
+  return -2.0 * s;
+}
+
+/* grad[i, 1] (qaoa.py:65-69): -2 Re <h| (-i C) lam> (state.py:319-321). */
+static double grad_gamma(const cplx* h, const cplx* v, const double* C, int64_t N) {
+  double s = 0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (int64_t x = 0; x < N; x++) s += creal(conj(h[x]) * (v[x] * (-I * C[x])));
+  return -2.0 * s;
+}
+
 /* Qaoa.grad_run (qaoa.py:40-70).  grad[i,0] is d/d beta_i, grad[i,1] is
- * d/d gamma_i; E uses the classical Hamiltonian (qaoa.py:56-57). */
-int qgo_qaoa_grad(int n, int p, const double* betas, const double* gammas, int nterms, const int* kind,
-                  const int* q0, const int* q1, const double* w, const double* ini, double* E, double* grad) {
+ * d/d gamma_i; E uses the classical Hamiltonian (qaoa.py:56-57).  mode 0
+ * keeps the reference's history of 2p+1 states; mode 1 uncomputes psi
+ * alongside lambda (inverse mixer, inverse cost phase). */
+static int qaoa_grad_impl(int n, int p, const double* betas, const double* gammas, int nterms, const int* kind,
+                          const int* q0, const int* q1, const double* w, const double* ini, double* E, double* grad,
+                          int uncompute) {
   if (n < 1 || n > 34 || p < 0) return QGO_EINVAL;
   const int64_t N = (int64_t)1 << n;
-  cplx* hist = (cplx*)malloc(sizeof(cplx) * (size_t)N * (size_t)(2 * p + 1));
+  const size_t nh = uncompute ? 1 : (size_t)(2 * p + 1);
+  cplx* hist = (cplx*)malloc(sizeof(cplx) * (size_t)N * nh);
   cplx* v = (cplx*)malloc(sizeof(cplx) * (size_t)N);
-  cplx* tmp = (cplx*)malloc(sizeof(cplx) * (size_t)N);
   double* C = (double*)malloc(sizeof(double) * (size_t)N);
-  if (!hist || !v || !tmp || !C) {
+  if (!hist || !v || !C) {
     free(hist);
     free(v);
-    free(tmp);
     free(C);
     return QGO_ENOMEM;
   }
+  cplx* psi = hist;
   classical_ham(C, n, nterms, kind, q0, q1, w);
   qaoa_start(v, n, ini);
   for (int i = 0; i < p; i++) {
-    memcpy(hist + (size_t)(2 * i) * N, v, sizeof(cplx) * (size_t)N);
+    if (!uncompute) memcpy(hist + (size_t)(2 * i) * N, v, sizeof(cplx) * (size_t)N);
     exp_ham(v, C, N, gammas[i]);
-    memcpy(hist + (size_t)(2 * i + 1) * N, v, sizeof(cplx) * (size_t)N);
+    if (!uncompute) memcpy(hist + (size_t)(2 * i + 1) * N, v, sizeof(cplx) * (size_t)N);
     for (int q = 0; q < n; q++) rot_xy(v, n, q, QGO_X, betas[i]);
   }
-  memcpy(hist + (size_t)(2 * p) * N, v, sizeof(cplx) * (size_t)N);
+  cplx* last = uncompute ? psi : hist + (size_t)(2 * p) * N;
+  memcpy(last, v, sizeof(cplx) * (size_t)N);
 #pragma omp parallel for schedule(static)
   for (int64_t x = 0; x < N; x++) v[x] *= C[x];
-  *E = re_vdot(hist + (size_t)(2 * p) * N, v, N);
+  *E = re_vdot(last, v, N);
   for (int i = p - 1; i >= 0; i--) {
     for (int q = 0; q < n; q++) rot_xy(v, n, q, QGO_X, -betas[i]);
-    memcpy(tmp, v, sizeof(cplx) * (size_t)N);
-    /* x_summed: v <- 1/2 sum_q (-i X_q) v (state.py:107-123) */
-#pragma omp parallel for schedule(static)
-    for (int64_t x = 0; x < N; x++) {
-      cplx acc = 0;
-      for (int q = 0; q < n; q++) acc += 0.5 * (-I) * tmp[x ^ ((int64_t)1 << bitpos(n, q))];
-      v[x] = acc;
-    }
-    grad[2 * i + 0] = -2.0 * re_vdot(hist + (size_t)(2 * i + 1) * N, v, N);
-    memcpy(v, tmp, sizeof(cplx) * (size_t)N);
+    if (uncompute)
+      for (int q = 0; q < n; q++) rot_xy(psi, n, q, QGO_X, -betas[i]);
+    grad[2 * i + 0] = grad_beta(uncompute ? psi : hist + (size_t)(2 * i + 1) * N, v, n);
     exp_ham(v, C, N, -gammas[i]);
-    memcpy(tmp, v, sizeof(cplx) * (size_t)N);
-#pragma omp parallel for schedule(static)
-    for (int64_t x = 0; x < N; x++) v[x] *= -I * C[x];
-    grad[2 * i + 1] = -2.0 * re_vdot(hist + (size_t)(2 * i) * N, v, N);
-    memcpy(v, tmp, sizeof(cplx) * (size_t)N);
+    if (uncompute) exp_ham(psi, C, N, -gammas[i]);
+    grad[2 * i + 1] = grad_gamma(uncompute ? psi : hist + (size_t)(2 * i) * N, v, C, N);
   }
   free(hist);
   free(v);
-  free(tmp);
   free(C);
   return QGO_OK;
+}
+
+int qgo_qaoa_grad(int n, int p, const double* betas, const double* gammas, int nterms, const int* kind,
+                  const int* q0, const int* q1, const double* w, const double* ini, double* E, double* grad) {
+  return qaoa_grad_impl(n, p, betas, gammas, nterms, kind, q0, q1, w, ini, E, grad, 0);
+}
+
+int qgo_qaoa_grad_uncompute(int n, int p, const double* betas, const double* gammas, int nterms, const int* kind,
+                            const int* q0, const int* q1, const double* w, const double* ini, double* E,
+                            double* grad) {
+  return qaoa_grad_impl(n, p, betas, gammas, nterms, kind, q0, q1, w, ini, E, grad, 1);
 }
 
 /* Entangler alone, for tests of the ladder permutation. */

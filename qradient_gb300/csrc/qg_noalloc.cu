@@ -1,22 +1,33 @@
 // qg_grad_noalloc: McClean / QAOA adjoint gradient with library-owned scratch.
 //
 // Some callers cannot call cudaMalloc on the path where they need a
-// gradient: code that runs while a CUDA stream is being captured into a
-// graph, plug-ins whose host process owns every device allocation through
-// its own pool, and real-time loops that forbid allocation after start-up.
-// This entry point takes the same inputs and outputs as qg_grad but needs
-// no workspace from the caller: its scratch is one file-scope device array,
-// reserved when the library is loaded and held by every GPU that loads it
-// until the process exits.
+// gradient: plug-ins whose host process owns every device allocation
+// through its own pool (it reserves the device memory up front, so a
+// library allocation either fails or escapes the host's accounting), and
+// real-time loops that forbid allocation after start-up (cudaMalloc may
+// synchronise the device and takes an unbounded time).  This entry point
+// takes the same inputs and outputs as qg_grad but needs no workspace from
+// the caller: its scratch is one file-scope device array, which every GPU
+// that loads the library's device code holds until the process exits.
+// With CUDA's lazy module loading that happens at the library's first
+// kernel launch or symbol lookup on the device, not when the shared
+// library is opened.
 //
 // The array is QG_NOALLOC_SCRATCH_BYTES (16 MiB).  A circuit fits when its
 // uncompute-mode workspace (qg_workspace_size with QG_OP_GRAD_UNCOMPUTE)
-// does; larger circuits get QG_ERR_UNSUPPORTED.  Nothing in the scratch has
-// to start at zero: the gradient pass clears its partial sums itself and
-// writes every state before reading it.  All calls on a device share the
-// array and it keeps the previous call's contents, so calls whose work
-// overlaps on the GPU (different streams, or several host threads) race;
-// callers must order them, for example on one stream.
+// does; larger circuits get QG_ERR_UNSUPPORTED before anything is launched.
+// Nothing in the scratch has to start at zero: the gradient pass clears its
+// partial sums itself and writes every state before reading it.  All calls
+// on a device share the array and it keeps the previous call's contents, so
+// calls whose work overlaps on the GPU (different streams, or several host
+// threads) race; callers must order them, for example on one stream.
+//
+// The array's device address is looked up once per device (the first call
+// on that device, with it current) and cached for the life of the process.
+// A context reset (cudaDeviceReset, or a primary context that is released
+// and created again) reloads the module, possibly at another address, and
+// invalidates the cached one: such a caller must not use this entry point
+// after the reset.
 #include <cuda_runtime.h>
 
 #include <mutex>

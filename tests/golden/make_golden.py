@@ -2,14 +2,15 @@
 
 Runs the reference's *unmodified* circuit logic
 (``qradient/circuit_logic/mc_clean.py``, ``qaoa.py``, ``base.py``) from a
-checkout given by ``--reference`` (default ``/root/reference``), with
+checkout given by ``--reference`` (or the ``QRADIENT_REFERENCE`` environment
+variable; one of the two is required), with
 ``ref_shim.py`` standing in for the ``qradient.physical_components`` classes
 the snapshot lacks.  Inputs are seeded (``numpy.random.default_rng``) and
 stored beside the outputs, so the tests never need the reference.
 
-Usage:  python tests/golden/make_golden.py [--reference PATH] [--big]
-        python tests/golden/make_golden.py --optimizer [--reference PATH]
-        python tests/golden/make_golden.py --projectors [--reference PATH]
+Usage:  python tests/golden/make_golden.py --reference PATH [--big]
+        python tests/golden/make_golden.py --optimizer --reference PATH
+        python tests/golden/make_golden.py --projectors --reference PATH
 
 ``--big`` adds the McClean ZZ-chain cases at n = 18, 20 (L = 50), which take
 about two minutes of reference time.
@@ -301,11 +302,14 @@ def projectors_main(reference):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("QRADIENT_REFERENCE"),
+                    help="path of a qradient checkout (or set QRADIENT_REFERENCE)")
     ap.add_argument("--big", action="store_true")
     ap.add_argument("--optimizer", action="store_true")
     ap.add_argument("--projectors", action="store_true")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("--reference PATH (or QRADIENT_REFERENCE) is required")
     if args.projectors:
         return projectors_main(args.reference)
     if args.optimizer:

@@ -95,3 +95,33 @@ def test_finite_differences_on_oracle():
                 em = O.mcclean_run(n, axes, a, t, entangler=ent, placement=place)
                 fd[i, q] = (ep - em) / (2 * h)
         assert np.max(np.abs(fd - g)) < 1e-8
+
+
+def test_uncompute_mode_matches_history_and_reference(golden):
+    """The oracle's uncompute mode (one psi taken backwards, used where the
+    L+1 stored states do not fit in host memory) against its history mode
+    and the reference's goldens, for every entangler and placement."""
+    for m in golden.cases("mcclean"):
+        if m["n"] > 14:
+            continue
+        c = golden.case("mcclean", m["name"])
+        ent = O.ENT_CZ if m["ladder"] == "cz" else O.ENT_CNOT
+        E, g = O.mcclean_grad(m["n"], c["axes"], c["angles"], _terms(c), entangler=ent, ini=c.get("ini"),
+                              uncompute=True)
+        assert abs(E - float(c["e_grad"])) <= TOL * max(1.0, abs(float(c["e_grad"]))), m["name"]
+        assert rel_err(g, c["grad"]) <= TOL, (m["name"], rel_err(g, c["grad"]))
+    n, L = 11, 7
+    rng = np.random.default_rng(11)
+    axes = rng.integers(0, 3, (L, n))
+    angles = rng.uniform(0, 2 * np.pi, (L, n))
+    t = O.Terms([3, 3, 0, 1, 2], [0, 4, 2, 9, 5], [1, 10, 2, 9, 5], [1.0, -0.5, 0.4, 0.3, 0.7])
+    for ent in (O.ENT_NONE, O.ENT_CNOT, O.ENT_CZ):
+        for place in (O.PLACE_BEFORE, O.PLACE_AFTER):
+            Eh, gh = O.mcclean_grad(n, axes, angles, t, entangler=ent, placement=place)
+            Eu, gu = O.mcclean_grad(n, axes, angles, t, entangler=ent, placement=place, uncompute=True)
+            assert abs(Eu - Eh) <= TOL and rel_err(gu, gh) <= TOL, (ent, place, rel_err(gu, gh))
+    for m in golden.cases("qaoa"):
+        c = golden.case("qaoa", m["name"])
+        E, g = O.qaoa_grad(m["n"], c["betas"], c["gammas"], _terms(c), ini=c.get("ini"), uncompute=True)
+        assert abs(E - float(c["e_grad"])) <= TOL * max(1.0, abs(float(c["e_grad"]))), m["name"]
+        assert rel_err(g, c["grad"]) <= TOL, (m["name"], rel_err(g, c["grad"]))

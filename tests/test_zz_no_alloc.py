@@ -1,8 +1,9 @@
 """qg_grad_noalloc: the allocation-free gradient entry point.
 
 It serves callers that cannot allocate device memory when they need a
-gradient (a stream being captured into a CUDA graph, a host process that
-owns every device allocation, a loop that must not allocate after start-up).
+gradient: a host process that owns every device allocation through its own
+pool, or a real-time loop that must not allocate (cudaMalloc may
+synchronise the device) after start-up.
 Its scratch is a fixed static device array inside the library, so the caller
 passes only inputs and outputs.  This test calls it through the C ABI twice
 in a row and checks each result against qg_grad with a caller-provided
