@@ -18,6 +18,14 @@ dtype) arrive over time.  Each scheduling round:
 
 Results are identical to running the request alone (same kernels, same
 reduction order); ``tests/test_gpu_serving.py`` checks this.
+
+Failures stay per request: parameters of the wrong size or with non-finite
+values are rejected by ``submit`` (``ValueError``, as the reference's
+``Qaoa.__check_parameters`` raises for a wrong count); a launch or a
+workspace allocation that raises fails the requests of that launch
+(``Request.error`` holds the message, they go to ``failed``), returns their
+footprint and stream, and leaves the server usable.  ``cancel(rid)``
+withdraws a request that has not been admitted yet.
 """
 import collections
 import time
@@ -31,7 +39,7 @@ from .batched import CLUSTER_MAX, Batch
 
 class Request:
     __slots__ = ("rid", "circuit", "params", "op", "dtype", "t_arrival", "t_done", "expec", "grad", "state",
-                 "footprint", "_e", "_g", "_event", "_keep")
+                 "footprint", "error", "_e", "_g", "_event", "_keep")
 
     def __init__(self, rid, circuit, params, op="grad", dtype="complex128", t_arrival=None):
         self.rid = rid
@@ -46,6 +54,8 @@ class Request:
         self.expec = None
         self.grad = None
         self.footprint = 0
+        self.error = None
+        self._e = self._g = None
         self._event = None
         self._keep = None
 
@@ -56,6 +66,10 @@ class Request:
     @property
     def done(self):
         return self.t_done is not None
+
+    @property
+    def failed(self):
+        return self.error is not None
 
 
 def _state_bytes(n, dtype):
@@ -77,6 +91,8 @@ class Server:
         self.queue = collections.deque()
         self.inflight = []
         self.finished = []
+        self.failed = []
+        self.rejected = []  # (schedule index, exception) of serve() entries that submit refused
         self.streams = [torch.cuda.Stream(self.device) for _ in range(streams)]
         self.stream_busy = [None] * streams
         # batches of consecutive rounds go to different streams: a round's
@@ -88,12 +104,52 @@ class Server:
     # ------------------------------------------------------------ interface
     def submit(self, circuit, params, op="grad", dtype="complex128", t_arrival=None):
         r = Request(self._rid, circuit, params, op, dtype, t_arrival)
+        want = self._nparams(circuit)
+        if r.params.size != want:
+            raise ValueError("request needs %d parameters, got %d" % (want, r.params.size))
+        if not np.all(np.isfinite(r.params)):
+            raise ValueError("request parameters must be finite")
         self._rid += 1
         self._size(r)
         if r.footprint > self.budget:
             raise MemoryError("request needs %d bytes, above the server budget %d" % (r.footprint, self.budget))
         self.queue.append(r)
         return r
+
+    def cancel(self, rid):
+        """Withdraw a queued request; True if it was still waiting for
+        admission (it then goes to ``failed`` with error 'cancelled'),
+        False if it is already on the device or done."""
+        for r in self.queue:
+            if r.rid == rid:
+                self.queue.remove(r)
+                r.error = "cancelled"
+                r.t_done = time.perf_counter()
+                self.failed.append(r)
+                return True
+        return False
+
+    @staticmethod
+    def _nparams(circuit):
+        kind = circuit.__class__.__name__
+        if kind == "McClean":
+            return circuit.lnum * circuit.qnum
+        if kind == "Qaoa":
+            return 2 * circuit.lnum
+        raise ValueError("expected a McClean or Qaoa circuit")
+
+    def _fail(self, reqs, exc):
+        """Fail `reqs` after their launch raised: record the error, return
+        their footprint, free their workspaces."""
+        now = time.perf_counter()
+        for r in reqs:
+            r.error = "%s: %s" % (type(exc).__name__, exc)
+            r.t_done = now
+            r._e = r._g = None
+            self.in_use -= r.footprint
+            self.failed.append(r)
+            if r.circuit._native is not None:
+                r.circuit._native.release_workspaces()
 
     def _small(self, r):
         kind = r.circuit.__class__.__name__
@@ -170,31 +226,39 @@ class Server:
         self._next_batch_stream = (self._next_batch_stream + 1) % len(self.batch_streams)
         with torch.cuda.stream(st):
             for dt, rs in by_dtype.items():
-                b = Batch(device=self.device, dtype=dt, grad=any(r.op == "grad" for r in rs), use_graph=False)
-                for r in rs:
-                    b.add(r.circuit, params=r.params.reshape(-1))
-                b.finalize()
-                b.execute()
-                ev = torch.cuda.Event()
-                ev.record(st)
+                try:
+                    b = Batch(device=self.device, dtype=dt, grad=any(r.op == "grad" for r in rs), use_graph=False)
+                    for r in rs:
+                        b.add(r.circuit, params=r.params.reshape(-1))
+                    b.finalize()
+                    b.execute()
+                    ev = torch.cuda.Event()
+                    ev.record(st)
+                except Exception as exc:  # the batch's requests fail, the server carries on
+                    self._fail(rs, exc)
+                    continue
                 self.inflight.append((ev, rs, b))
 
     def _launch_large(self, r):
         idx = next(i for i, s in enumerate(self.stream_busy) if s is None)
         st = self.streams[idx]
-        nat = r.circuit.native()
-        with torch.cuda.stream(st):
-            params = torch.as_tensor(r.params.reshape(-1)).to(self.device, non_blocking=False)
-            if r.op == "grad":
-                ws = nat.workspace(r.dtype, _lib.QG_OP_GRAD_UNCOMPUTE, self.device)
-                e, g = nat.grad(params, r.dtype, self.device, _lib.QG_OP_GRAD_UNCOMPUTE, workspace=ws)
-            else:
-                ws = nat.workspace(r.dtype, _lib.QG_OP_RUN, self.device)
-                e, _ = nat.run(params, r.dtype, self.device, workspace=ws)
-                g = None
-            r._e, r._g = e, g
-            ev = torch.cuda.Event()
-            ev.record(st)
+        try:
+            nat = r.circuit.native()
+            with torch.cuda.stream(st):
+                params = torch.as_tensor(r.params.reshape(-1)).to(self.device, non_blocking=False)
+                if r.op == "grad":
+                    ws = nat.workspace(r.dtype, _lib.QG_OP_GRAD_UNCOMPUTE, self.device)
+                    e, g = nat.grad(params, r.dtype, self.device, _lib.QG_OP_GRAD_UNCOMPUTE, workspace=ws)
+                else:
+                    ws = nat.workspace(r.dtype, _lib.QG_OP_RUN, self.device)
+                    e, _ = nat.run(params, r.dtype, self.device, workspace=ws)
+                    g = None
+                r._e, r._g = e, g
+                ev = torch.cuda.Event()
+                ev.record(st)
+        except Exception as exc:  # this request fails, its stream stays free
+            self._fail([r], exc)
+            return
         item = (ev, [r], (params, ws))
         self.stream_busy[idx] = item
         self.inflight.append(item)
@@ -210,6 +274,7 @@ class Server:
         return len(small) + len(large)
 
     def drain(self, timeout=600.0):
+        """Step until every request has finished or failed; returns the finished ones."""
         t0 = time.perf_counter()
         while self.queue or self.inflight:
             if not self.step():
@@ -229,7 +294,10 @@ class Server:
             now = time.perf_counter() - t0
             while i < len(schedule) and schedule[i][0] <= now:
                 off, c, p, op, dt = schedule[i]
-                self.submit(c, p, op, dt, t_arrival=t0 + off)
+                try:
+                    self.submit(c, p, op, dt, t_arrival=t0 + off)
+                except (ValueError, MemoryError) as exc:  # refused at the door; the stream goes on
+                    self.rejected.append((i, exc))
                 i += 1
             if not self.step():
                 time.sleep(0.0002)
