@@ -795,8 +795,8 @@ def main():
         line["cz_after"] = measure_mcclean(args.n, args.layers, args.seed, args.dtype, "cz", "after", 5, 3, dev)
         line["qaoa"] = _public(measure_qaoa(24, 10, 24, "complex128", 5, 3, dev))
         line["batched"] = measure_batched(14, 30, 4096, "complex64", 5, 3, 14, dev, e2e=True)
-        line["served"] = {"small": measure_served(24, 200, 14, args.streams, dev),
-                          "full": measure_served(26, 40, 26, args.streams, dev)}
+        line["served"] = {"small": measure_served(24, 1000, 14, args.streams, dev),
+                          "full": measure_served(26, 60, 26, args.streams, dev)}
         line["extras_clocks"] = extra_clk.stop()
         line["extras_wall_s"] = time.perf_counter() - t0
     if rank == 0 and not args.no_cpu_baseline:

@@ -196,10 +196,22 @@ static void apply_observable(const cplx* v, cplx* out, int n, int nterms, const 
   }
 }
 
+/* Sums below run in blocks of QGO_BLOCK elements: each block is summed on
+ * its own, then the block sums are added, as BLAS dot products accumulate in
+ * several partial sums (numpy's vdot, base.py:17-20 and mc_clean.py:66,74).
+ * A single running sum over 2^30 elements would lose about 1e-11 of
+ * absolute accuracy. */
+#define QGO_BLOCK 4096
+
 static double re_vdot(const cplx* a, const cplx* b, int64_t N) {
   double s = 0;
 #pragma omp parallel for reduction(+ : s) schedule(static)
-  for (int64_t x = 0; x < N; x++) s += creal(conj(a[x]) * b[x]);
+  for (int64_t x0 = 0; x0 < N; x0 += QGO_BLOCK) {
+    const int64_t x1 = x0 + QGO_BLOCK < N ? x0 + QGO_BLOCK : N;
+    double bs = 0;
+    for (int64_t x = x0; x < x1; x++) bs += creal(conj(a[x]) * b[x]);
+    s += bs;
+  }
   return s;
 }
 
@@ -268,11 +280,16 @@ static double grad_entry(const cplx* h, const cplx* v, int n, int q, int axis, d
     const int64_t N = (int64_t)1 << n;
     const int64_t bp = bitpos(n, q);
 #pragma omp parallel for reduction(+ : s) schedule(static)
-    for (int64_t x = 0; x < N; x++) {
-      const int one = (int)((x >> bp) & 1);
-      const cplx r = v[x] * (one ? r1 : r0);
-      const cplx d = r * (one ? d1 : d0);
-      s += creal(conj(h[x]) * d);
+    for (int64_t x0 = 0; x0 < N; x0 += QGO_BLOCK) {
+      const int64_t x1 = x0 + QGO_BLOCK < N ? x0 + QGO_BLOCK : N;
+      double bs = 0;
+      for (int64_t x = x0; x < x1; x++) {
+        const int one = (int)((x >> bp) & 1);
+        const cplx r = v[x] * (one ? r1 : r0);
+        const cplx d = r * (one ? d1 : d0);
+        bs += creal(conj(h[x]) * d);
+      }
+      s += bs;
     }
     return -2.0 * s;
   }
@@ -281,28 +298,33 @@ static double grad_entry(const cplx* h, const cplx* v, int n, int q, int axis, d
   const int64_t half = (int64_t)1 << (n - 1);
   const int64_t stride = (int64_t)1 << bitpos(n, q);
 #pragma omp parallel for reduction(+ : s) schedule(static)
-  for (int64_t k = 0; k < half; k++) {
-    const int64_t a = ((k & ~(stride - 1)) << 1) | (k & (stride - 1));
-    const int64_t b = a | stride;
-    const cplx va = v[a], vb = v[b];
-    cplx pa, pb;
-    if (axis == QGO_X) {
-      pa = -I * vb;
-      pb = -I * va;
-    } else {
-      pa = -vb;
-      pb = va;
+  for (int64_t k0 = 0; k0 < half; k0 += QGO_BLOCK) {
+    const int64_t k1 = k0 + QGO_BLOCK < half ? k0 + QGO_BLOCK : half;
+    double bs = 0;
+    for (int64_t k = k0; k < k1; k++) {
+      const int64_t a = ((k & ~(stride - 1)) << 1) | (k & (stride - 1));
+      const int64_t b = a | stride;
+      const cplx va = v[a], vb = v[b];
+      cplx pa, pb;
+      if (axis == QGO_X) {
+        pa = -I * vb;
+        pb = -I * va;
+      } else {
+        pa = -vb;
+        pb = va;
+      }
+      const cplx ra = rs * pa + rc * va, rb = rs * pb + rc * vb;
+      if (axis == QGO_X) {
+        pa = -I * rb;
+        pb = -I * ra;
+      } else {
+        pa = -rb;
+        pb = ra;
+      }
+      const cplx da = 0.5 * dc * pa - 0.5 * ds * ra, db = 0.5 * dc * pb - 0.5 * ds * rb;
+      bs += creal(conj(h[a]) * da) + creal(conj(h[b]) * db);
     }
-    const cplx ra = rs * pa + rc * va, rb = rs * pb + rc * vb;
-    if (axis == QGO_X) {
-      pa = -I * rb;
-      pb = -I * ra;
-    } else {
-      pa = -rb;
-      pb = ra;
-    }
-    const cplx da = 0.5 * dc * pa - 0.5 * ds * ra, db = 0.5 * dc * pb - 0.5 * ds * rb;
-    s += creal(conj(h[a]) * da) + creal(conj(h[b]) * db);
+    s += bs;
   }
   return -2.0 * s;
 }
@@ -468,10 +490,15 @@ static double grad_beta(const cplx* h, const cplx* v, int n) {
   const int64_t N = (int64_t)1 << n;
   double s = 0;
 #pragma omp parallel for reduction(+ : s) schedule(static)
-  for (int64_t x = 0; x < N; x++) {
-    cplx acc = 0;
-    for (int q = 0; q < n; q++) acc += 0.5 * (-I) * v[x ^ ((int64_t)1 << bitpos(n, q))];
-    s += creal(conj(h[x]) * acc);
+  for (int64_t x0 = 0; x0 < N; x0 += QGO_BLOCK) {
+    const int64_t x1 = x0 + QGO_BLOCK < N ? x0 + QGO_BLOCK : N;
+    double bs = 0;
+    for (int64_t x = x0; x < x1; x++) {
+      cplx acc = 0;
+      for (int q = 0; q < n; q++) acc += 0.5 * (-I) * v[x ^ ((int64_t)1 << bitpos(n, q))];
+      bs += creal(conj(h[x]) * acc);
+    }
+    s += bs;
   }
   return -2.0 * s;
 }
@@ -480,7 +507,12 @@ static double grad_beta(const cplx* h, const cplx* v, int n) {
 static double grad_gamma(const cplx* h, const cplx* v, const double* C, int64_t N) {
   double s = 0;
 #pragma omp parallel for reduction(+ : s) schedule(static)
-  for (int64_t x = 0; x < N; x++) s += creal(conj(h[x]) * (v[x] * (-I * C[x])));
+  for (int64_t x0 = 0; x0 < N; x0 += QGO_BLOCK) {
+    const int64_t x1 = x0 + QGO_BLOCK < N ? x0 + QGO_BLOCK : N;
+    double bs = 0;
+    for (int64_t x = x0; x < x1; x++) bs += creal(conj(h[x]) * (v[x] * (-I * C[x])));
+    s += bs;
+  }
   return -2.0 * s;
 }
 
