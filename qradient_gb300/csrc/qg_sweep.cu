@@ -1137,14 +1137,11 @@ cudaError_t prepare_sweep_kernels() {
                        (const void*)sweep_fwd_kernel<float>,
                        (const void*)sweep_fwd_pipe_kernel<double, 0>,
                        (const void*)sweep_fwd_pipe_kernel<float, 0>,
-                       (const void*)sweep_fwd_pipe_kernel<float, kTileC64>,
                        (const void*)sweep_fwd_pipe_kernel<double, kTileC128>,
                        (const void*)sweep_bwd_kernel<double, false, 0>,
                        (const void*)sweep_bwd_kernel<double, true, 0>,
                        (const void*)sweep_bwd_kernel<float, false, 0>,
                        (const void*)sweep_bwd_kernel<float, true, 0>,
-                       (const void*)sweep_bwd_kernel<float, false, kTileC64>,
-                       (const void*)sweep_bwd_kernel<float, true, kTileC64>,
                        (const void*)sweep_bwd_kernel<double, false, kTileC128>,
                        (const void*)sweep_bwd_kernel<double, true, kTileC128>,
                        (const void*)observable_kernel<double>,
@@ -1153,32 +1150,43 @@ cudaError_t prepare_sweep_kernels() {
     e = set_smem_limit(fn, optin);
     if (e != cudaSuccess) return e;
   }
+  e = prepare_reg_sweep_kernels(optin);
+  if (e != cudaSuccess) return e;
   ready[dev].store(1, std::memory_order_release);
   return cudaSuccess;
 }
 
-// The kernel a sweep launches: sweeps over tiles of the default size take
-// the instantiation with the tile size fixed at compile time.
+// The kernel a sweep launches.  complex64 sweeps over 12-bit tiles (the
+// default) run in the register-layout kernels (qg_sweep_reg.cu); complex128
+// sweeps over tiles of the default size take the instantiation with the
+// tile size fixed at compile time; other tiles the runtime-size kernels.
 template <typename R>
 static bool fixed_tile(const SweepDesc& d) {
-  return d.t == kTileFixed<R>;
+  return sizeof(R) == 8 && d.t == kTileC128;
+}
+template <typename R>
+static bool reg_sweep(const SweepDesc& d, bool bwd) {
+  return sizeof(R) == 4 && reg_sweep_applies(d, bwd);
 }
 template <typename R>
 static const void* fwd_pipe_fn(const SweepDesc& d) {
-  if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<R, kTileFixed<R>>;
+  if (reg_sweep<R>(d, false)) return reg_sweep_fn(d, false, false);
+  if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<double, kTileC128>;
   return (const void*)sweep_fwd_pipe_kernel<R, 0>;
 }
 template <typename R>
 static const void* bwd_fn(const SweepDesc& d, bool uncompute) {
+  if (reg_sweep<R>(d, true)) return reg_sweep_fn(d, true, uncompute);
   if (fixed_tile<R>(d))
-    return uncompute ? (const void*)sweep_bwd_kernel<R, true, kTileFixed<R>>
-                     : (const void*)sweep_bwd_kernel<R, false, kTileFixed<R>>;
+    return uncompute ? (const void*)sweep_bwd_kernel<double, true, kTileC128>
+                     : (const void*)sweep_bwd_kernel<double, false, kTileC128>;
   return uncompute ? (const void*)sweep_bwd_kernel<R, true, 0> : (const void*)sweep_bwd_kernel<R, false, 0>;
 }
 
 template <typename R>
 int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe) {
-  const size_t smem = sweep_smem<R>(d, bwd, pipe && !bwd);
+  const bool reg = reg_sweep<R>(d, bwd) && (bwd || pipe);
+  const size_t smem = reg ? reg_sweep_smem(d) : sweep_smem<R>(d, bwd, pipe && !bwd);
   int blocks = 0;
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) {
@@ -1203,8 +1211,12 @@ cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   if (pipe && d.start == START_LOAD) {
-    if (fixed_tile<R>(d))
-      return launch_pdl(sweep_fwd_pipe_kernel<R, kTileFixed<R>>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
+    if constexpr (sizeof(R) == 4) {
+      if (reg_sweep<R>(d, false)) return launch_reg_sweep_fwd(d, p, grid, st, pdl);
+    } else {
+      if (fixed_tile<R>(d))
+        return launch_pdl(sweep_fwd_pipe_kernel<double, kTileC128>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
+    }
     return launch_pdl(sweep_fwd_pipe_kernel<R, 0>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
   }
   return launch_pdl(sweep_fwd_kernel<R>, grid, sweep_smem<R>(d, false), st, pdl, d, p);
@@ -1216,9 +1228,13 @@ cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool unc
   const size_t smem = sweep_smem<R>(d, true);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
-  if (fixed_tile<R>(d)) {
-    if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, kTileFixed<R>>, grid, smem, st, pdl, d, p);
-    return launch_pdl(sweep_bwd_kernel<R, false, kTileFixed<R>>, grid, smem, st, pdl, d, p);
+  if constexpr (sizeof(R) == 4) {
+    if (reg_sweep<R>(d, true)) return launch_reg_sweep_bwd(d, p, uncompute, grid, st, pdl);
+  } else {
+    if (fixed_tile<R>(d)) {
+      if (uncompute) return launch_pdl(sweep_bwd_kernel<double, true, kTileC128>, grid, smem, st, pdl, d, p);
+      return launch_pdl(sweep_bwd_kernel<double, false, kTileC128>, grid, smem, st, pdl, d, p);
+    }
   }
   if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, 0>, grid, smem, st, pdl, d, p);
   return launch_pdl(sweep_bwd_kernel<R, false, 0>, grid, smem, st, pdl, d, p);
