@@ -36,12 +36,12 @@ cudaError_t launch_cost_reduce(int n, const typename C2T<R>::T* lam, const typen
                                int cost, double w0, const int32_t* cost_i, const double* cost_d, double* partials,
                                int slot, int G, cudaStream_t st);
 
-// complex64 register-layout sweeps (qg_sweep_reg.cu): sweeps over 12-bit
-// tiles (forward ones that load their input, and every backward one) run
-// there.  The shared-memory round trips of a sweep (0..2) set its shared
-// memory and so its occupancy class.
+// complex64 register-layout sweeps (qg_sweep_reg.cu): the 12-bit-tile sweeps
+// over high qubits run there (reg_sweep_applies).  The shared-memory round
+// trips a sweep needs in register layouts (0..2) set its shared memory and
+// so its occupancy class.
 bool reg_sweep_applies(const SweepDesc& d, bool bwd);
-size_t reg_sweep_smem(const SweepDesc& d);
+size_t reg_sweep_smem(const SweepDesc& d, bool bwd);
 const void* reg_sweep_fn(const SweepDesc& d, bool bwd, bool uncompute);
 int sweep_occupancy_class(const SweepDesc& d);
 cudaError_t prepare_reg_sweep_kernels(int optin);

@@ -1137,11 +1137,14 @@ cudaError_t prepare_sweep_kernels() {
                        (const void*)sweep_fwd_kernel<float>,
                        (const void*)sweep_fwd_pipe_kernel<double, 0>,
                        (const void*)sweep_fwd_pipe_kernel<float, 0>,
+                       (const void*)sweep_fwd_pipe_kernel<float, kTileC64>,
                        (const void*)sweep_fwd_pipe_kernel<double, kTileC128>,
                        (const void*)sweep_bwd_kernel<double, false, 0>,
                        (const void*)sweep_bwd_kernel<double, true, 0>,
                        (const void*)sweep_bwd_kernel<float, false, 0>,
                        (const void*)sweep_bwd_kernel<float, true, 0>,
+                       (const void*)sweep_bwd_kernel<float, false, kTileC64>,
+                       (const void*)sweep_bwd_kernel<float, true, kTileC64>,
                        (const void*)sweep_bwd_kernel<double, false, kTileC128>,
                        (const void*)sweep_bwd_kernel<double, true, kTileC128>,
                        (const void*)observable_kernel<double>,
@@ -1156,13 +1159,14 @@ cudaError_t prepare_sweep_kernels() {
   return cudaSuccess;
 }
 
-// The kernel a sweep launches.  complex64 sweeps over 12-bit tiles (the
-// default) run in the register-layout kernels (qg_sweep_reg.cu); complex128
-// sweeps over tiles of the default size take the instantiation with the
-// tile size fixed at compile time; other tiles the runtime-size kernels.
+// The kernel a sweep launches.  complex64 sweeps over the high qubits of
+// 12-bit tiles (the default) run in the register-layout kernels
+// (qg_sweep_reg.cu, reg_sweep_applies); other sweeps over tiles of the
+// default size take the instantiation with the tile size fixed at compile
+// time; other tiles the runtime-size kernels.
 template <typename R>
 static bool fixed_tile(const SweepDesc& d) {
-  return sizeof(R) == 8 && d.t == kTileC128;
+  return d.t == kTileFixed<R>;
 }
 template <typename R>
 static bool reg_sweep(const SweepDesc& d, bool bwd) {
@@ -1171,22 +1175,22 @@ static bool reg_sweep(const SweepDesc& d, bool bwd) {
 template <typename R>
 static const void* fwd_pipe_fn(const SweepDesc& d) {
   if (reg_sweep<R>(d, false)) return reg_sweep_fn(d, false, false);
-  if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<double, kTileC128>;
+  if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<R, kTileFixed<R>>;
   return (const void*)sweep_fwd_pipe_kernel<R, 0>;
 }
 template <typename R>
 static const void* bwd_fn(const SweepDesc& d, bool uncompute) {
   if (reg_sweep<R>(d, true)) return reg_sweep_fn(d, true, uncompute);
   if (fixed_tile<R>(d))
-    return uncompute ? (const void*)sweep_bwd_kernel<double, true, kTileC128>
-                     : (const void*)sweep_bwd_kernel<double, false, kTileC128>;
+    return uncompute ? (const void*)sweep_bwd_kernel<R, true, kTileFixed<R>>
+                     : (const void*)sweep_bwd_kernel<R, false, kTileFixed<R>>;
   return uncompute ? (const void*)sweep_bwd_kernel<R, true, 0> : (const void*)sweep_bwd_kernel<R, false, 0>;
 }
 
 template <typename R>
 int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe) {
   const bool reg = reg_sweep<R>(d, bwd) && (bwd || pipe);
-  const size_t smem = reg ? reg_sweep_smem(d) : sweep_smem<R>(d, bwd, pipe && !bwd);
+  const size_t smem = reg ? reg_sweep_smem(d, bwd) : sweep_smem<R>(d, bwd, pipe && !bwd);
   int blocks = 0;
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) {
@@ -1213,10 +1217,9 @@ cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid
   if (pipe && d.start == START_LOAD) {
     if constexpr (sizeof(R) == 4) {
       if (reg_sweep<R>(d, false)) return launch_reg_sweep_fwd(d, p, grid, st, pdl);
-    } else {
-      if (fixed_tile<R>(d))
-        return launch_pdl(sweep_fwd_pipe_kernel<double, kTileC128>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
     }
+    if (fixed_tile<R>(d))
+      return launch_pdl(sweep_fwd_pipe_kernel<R, kTileFixed<R>>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
     return launch_pdl(sweep_fwd_pipe_kernel<R, 0>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
   }
   return launch_pdl(sweep_fwd_kernel<R>, grid, sweep_smem<R>(d, false), st, pdl, d, p);
@@ -1230,11 +1233,10 @@ cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool unc
   if (e != cudaSuccess) return e;
   if constexpr (sizeof(R) == 4) {
     if (reg_sweep<R>(d, true)) return launch_reg_sweep_bwd(d, p, uncompute, grid, st, pdl);
-  } else {
-    if (fixed_tile<R>(d)) {
-      if (uncompute) return launch_pdl(sweep_bwd_kernel<double, true, kTileC128>, grid, smem, st, pdl, d, p);
-      return launch_pdl(sweep_bwd_kernel<double, false, kTileC128>, grid, smem, st, pdl, d, p);
-    }
+  }
+  if (fixed_tile<R>(d)) {
+    if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, kTileFixed<R>>, grid, smem, st, pdl, d, p);
+    return launch_pdl(sweep_bwd_kernel<R, false, kTileFixed<R>>, grid, smem, st, pdl, d, p);
   }
   if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, 0>, grid, smem, st, pdl, d, p);
   return launch_pdl(sweep_bwd_kernel<R, false, 0>, grid, smem, st, pdl, d, p);

@@ -15,10 +15,11 @@
 
 namespace qg {
 
-// default complex128 tile bits (the size the shared-memory sweep kernels are
-// also instantiated for with the tile size fixed at compile time; the
-// complex64 default, 12 bits, runs in the register-layout kernels)
-constexpr int kTileC128 = 11;
+// default tile bits (the sizes the shared-memory sweep kernels are also
+// instantiated for with the tile size fixed at compile time)
+constexpr int kTileC64 = 12, kTileC128 = 11;
+template <typename R>
+constexpr int kTileFixed = sizeof(R) == 4 ? kTileC64 : kTileC128;
 
 // Programmatic dependent launch.  The sweep and observable kernels let the
 // next launch start at once (pdl_trigger) and, after their setup (which

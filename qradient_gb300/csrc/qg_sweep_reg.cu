@@ -1,32 +1,38 @@
 // complex64 register-layout sweeps: the forward and adjoint backward sweeps
-// of 12-bit tiles (the complex64 default) with every amplitude of a tile held
-// in registers, 16 per thread, instead of staged in shared memory.
+// over 12-bit tiles (the complex64 default) that rotate only the tile's high
+// bits -- the sweeps over the high qubits -- with every amplitude of a tile
+// held in registers, 16 per thread, instead of staged in shared memory.
 //
 // A tile is 4096 amplitudes, local index l = 12 bits (tile bit i is global
-// bit d.bits[i]).  A thread (lane, warp) of the 256-thread CTA holds 16 of
-// them in one of three layouts:
+// bit d.bits[i]; local bits 0..3 are the state's lowest bits).  A thread
+// (lane, warp) of the 256-thread CTA holds 16 of them in one of two layouts:
 //   L1: l = lane | warp << 5 | k << 8            in-thread bits 8..11
-//   L2: l = k | lane << 4 | warp << 9            in-thread bits 0..3
 //   L3: l = (lane & 15) | k << 4 | (lane >> 4) << 8 | warp << 9
 //                                                in-thread bits 4..7
-// Rotations on in-thread bits need no data movement, so a sweep runs in
-// phases: it loads its tile from global memory straight into L1 registers
-// (lanes run along local bits 0..4: coalesced), applies its rotations on bits
-// 8..11, moves to L2 through shared memory if it rotates bits 0..3, then to L3
-// if it rotates bits 4..7 (or came through L2), and stores from L1 or L3
-// (lanes along local bits 0..3: coalesced 128-byte runs).  A sweep over the
-// low 12 bits costs two shared-memory round trips per amplitude, a sweep over
-// 8 high bits one, a sweep over 4 high bits none -- against one per group of
-// rotations plus the load and store passes in the shared-memory kernels.
+// Rotations on in-thread bits need no data movement.  A sweep loads its
+// tile from global memory straight into L1 registers (lanes along local bits
+// 0..4: coalesced), applies its rotations on bits 8..11, moves to L3 through
+// shared memory if it also rotates bits 4..7, and stores from L1 or L3
+// (lanes along local bits 0..3: coalesced 128-byte runs).  The sweep over 4
+// high bits then costs no shared-memory pass at all and the one over 8 high
+// bits one round trip, against a load pass, a store pass and a pass per
+// group of rotations in the shared-memory kernels (qg_sweep.cu).
 //
-// Arithmetic is that of the shared-memory kernels (qg_sweep.cu): the scaled
-// rotation forms, the per-sweep diagonal (merged Z table times the layer
-// scale, cost phase, CZ sign) at the same point, the CNOT ladder as a gather
-// on load, and in the backward sweep Im<lam|P_q|psi> for every rotation of
-// the sweep at the sweep's end point (mc_clean.py:68-77, qaoa.py:59-69).
-// A phase's reductions are taken after the earlier phases' inverse rotations
-// have been applied to lambda and psi alike: the rotations of a layer commute
-// with each other's Paulis, so the sums are those at the end point, up to the
+// Where they run (measured per sweep at n = 24 on GB300): forward sweeps
+// that rotate bits 8..11 only (55 against 59 us), backward sweeps with at
+// most one round trip (82 against 94 us; 109 against 119 us).  The sweep
+// over the low 12 bits needs two round trips; in this form its unrolled
+// per-bit rotation code outgrew the instruction cache and it ran slower
+// than the shared-memory kernel, which it keeps.
+//
+// Arithmetic is that of the shared-memory kernels: the scaled rotation
+// forms, the per-sweep diagonal (merged Z table times the layer scale, cost
+// phase, CZ sign) at the same point, the CNOT ladder as a gather on load,
+// and in the backward sweep Im<lam|P_q|psi> for every rotation of the sweep
+// at the sweep's end point (mc_clean.py:68-77, qaoa.py:59-69).  The bits
+// 4..7 sums are taken after the bits 8..11 inverse rotations have been
+// applied to lambda and psi alike: the rotations of a layer commute with
+// each other's Paulis, so the sums are those at the end point, up to the
 // factor 1/kappa^2 each unscaled inverse rotation leaves on the product,
 // which is multiplied back per CTA.
 //
@@ -58,12 +64,6 @@ struct Lay<1> {
   __host__ __device__ static constexpr int kp(int k) { return k << 8; }
 };
 template <>
-struct Lay<2> {
-  static constexpr int BASE = 0;
-  __device__ static __forceinline__ int thr(int lane, int warp) { return (lane << 4) | (warp << 9); }
-  __host__ __device__ static constexpr int kp(int k) { return k; }
-};
-template <>
 struct Lay<3> {
   static constexpr int BASE = 4;
   __device__ static __forceinline__ int thr(int lane, int warp) {
@@ -73,10 +73,10 @@ struct Lay<3> {
 };
 
 // the complex64 shared-memory swizzle (sw<float>): GF(2)-linear, so the slot
-// of thread part | element part is the XOR of the parts' slots.  In every
-// layout the 16 lanes of a half warp differ in local bits 0..3 or 4..7, which
-// the swizzle maps onto 16 distinct 8-byte bank pairs: the 64-bit accesses of
-// a transpose are free of bank conflicts.
+// of thread part | element part is the XOR of the parts' slots.  In both
+// layouts the 16 lanes of a half warp differ in local bits 0..3, which the
+// swizzle maps onto 16 distinct 8-byte bank pairs: the 64-bit accesses of a
+// round trip are free of bank conflicts.
 __host__ __device__ constexpr int swf(int e) { return e ^ ((e >> 4) & 15); }
 
 template <int LAY>
@@ -123,8 +123,9 @@ __host__ __device__ __forceinline__ int rot_mask(const SweepDesc& d) {
   return m;
 }
 
-// shared-memory round trips of a sweep: 0 (rotations on bits 8..11 only),
-// 1 (L1 -> L3: rotations on bits 4..7 as well), 2 (L1 -> L2 -> L3)
+// shared-memory round trips a sweep would need in register layouts: 0
+// (rotations on bits 8..11 only), 1 (L1 -> L3: bits 4..7 as well), 2 (bits
+// 0..3 as well: a further layout with in-thread bits 0..3)
 __host__ __device__ __forceinline__ int reg_transposes(const SweepDesc& d) {
   const int m = rot_mask(d);
   return (m & 0x00f) ? 2 : (m & 0x0f0) ? 1 : 0;
@@ -196,18 +197,15 @@ __device__ __forceinline__ Parts make_parts(const SweepDesc& d) {
 
 // ------------------------------------------------------------ forward
 
-// NT: shared-memory round trips of this sweep (reg_transposes).  Three CTAs
-// of 256 threads per SM; the tile buffers (two, when NT > 0) alternate so
-// that one barrier per round trip suffices.
-template <int NT>
+// Sweeps rotating bits 8..11 only: load, rotate and store in L1 registers.
+// Three CTAs of 256 threads per SM.
 __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_reg_kernel(const __grid_constant__ SweepDesc d,
                                                                     SweepPtrs<float> p) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SetupShared S;
   __shared__ RegShared R;
   __shared__ int64_t ladk[32];
-  float2* buf = (float2*)smem;
-  float2* ztab = buf + (NT > 0 ? 2 * RTS : 0);
+  float2* ztab = (float2*)smem;
   float2* ctab = ztab + (1 << d.nz);
   sweep_setup<float2, false>(d, p.params, S, ztab, ctab, ladk);
   reg_setup(d, S, R);
@@ -223,8 +221,7 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_reg_kernel(const __grid
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
   const bool diag_pass = d.cost != COST_NONE || d.pre == ENT_CZ;
   const bool diag_store = !diag_pass && d.has_diag;
-  const int mk = rot_mask(d);
-  const int m1 = (mk >> 8) & 15, m2 = mk & 15, m3 = (mk >> 4) & 15;
+  const int m1 = (rot_mask(d) >> 8) & 15;
 
   const Parts P1 = make_parts<1>(d);
   const int64_t t1 = deposit(Lay<1>::thr(lane, warp), d.bits, RT);
@@ -233,16 +230,12 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_reg_kernel(const __grid
 #pragma unroll
   for (int i = 0; i < 4; ++i) lk[i] = (int64_t)ladder_inv((uint64_t)P1.o[i], lm);
   const uint64_t lt1 = ladder_inv((uint64_t)t1, lm);
-  const Parts P3 = make_parts<3>(d);
-  const int64_t t3 = deposit(Lay<3>::thr(lane, warp), d.bits, RT);
-  const int z3 = zpattern((uint64_t)t3, d);
-  const int s1 = swf(Lay<1>::thr(lane, warp)), s2 = swf(Lay<2>::thr(lane, warp)), s3 = swf(Lay<3>::thr(lane, warp));
   TileBases tb(S.outside, n - RT, n, d.bits, RT);
 
-  int parity = 0;
   for (int64_t tileid = blockIdx.x; tileid < ntiles; tileid += gridDim.x) {
     const int64_t base = tb.advance();
-    const int zb = zpattern((uint64_t)base, d);
+    const uint64_t bd = (uint64_t)(base | t1);
+    const int zb = zpattern((uint64_t)base, d) | z1;
     float2 v[RK];
     // load in L1, gathered through the CNOT ladder when the sweep starts with it
     if (d.pre == ENT_CNOT) {
@@ -256,56 +249,32 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_reg_kernel(const __grid
         v[k] = p.psi_in[s];
       }
     } else {
-      const float2* pin = p.psi_in + (base | t1);
+      const float2* pin = p.psi_in + bd;
 #pragma unroll
       for (int k = 0; k < RK; ++k) v[k] = pin[part_off(P1, k)];
     }
     if (diag_pass) {
-      const uint64_t bd = (uint64_t)(base | t1);
 #pragma unroll
       for (int k = 0; k < RK; ++k) {
         const uint64_t x = bd + (uint64_t)part_off(P1, k);
         float2 e = v[k];
         if (d.pre == ENT_CZ && cz_negative(x)) e = cneg(e);
-        v[k] = apply_diag<float2>(e, x, zb | z1 | part_z(P1, k), d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold,
-                                  false);
+        v[k] = apply_diag<float2>(e, x, zb | part_z(P1, k), d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
       }
     }
     rot_phase<1, 8>(v, m1, R);
-    if (NT == 2) {
-      float2* b0 = buf;
-      to_smem<1>(b0, v, s1);
-      __syncthreads();
-      from_smem<2>(b0, v, s2);
-      rot_phase<1, 0>(v, m2, R);
-      float2* b1 = buf + RTS;
-      to_smem<2>(b1, v, s2);
-      __syncthreads();
-      from_smem<3>(b1, v, s3);
-    } else if (NT == 1) {
-      // one round trip per tile: the two buffers alternate between tiles, so
-      // a buffer is rewritten only after the next tile's barrier
-      float2* b = buf + parity * RTS;
-      to_smem<1>(b, v, s1);
-      __syncthreads();
-      from_smem<3>(b, v, s3);
-      parity ^= 1;
-    }
-    if (NT > 0) rot_phase<1, 4>(v, m3, R);
-    // store from L1 (NT == 0) or L3, with the diagonal when it commutes
-    const int64_t bo = base | (NT > 0 ? t3 : t1);
-    float2* out = p.psi_out + bo;
-    const int zo = zb | (NT > 0 ? z3 : z1);
+    // store from L1, with the diagonal when it commutes with the rotations
+    float2* out = p.psi_out + bd;
 #pragma unroll
     for (int k = 0; k < RK; ++k) {
-      const int64_t off = NT > 0 ? part_off(P3, k) : part_off(P1, k);
+      const int64_t off = part_off(P1, k);
       float2 e = v[k];
       if (diag_store) {
-        const int zp = zo | (NT > 0 ? part_z(P3, k) : part_z(P1, k));
+        const int zp = zb | part_z(P1, k);
         if (d.cost == COST_NONE && d.nz > 0)
           e = cmul(e, ztab[zp]);
         else
-          e = apply_diag<float2>(e, (uint64_t)(bo + off), zp, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
+          e = apply_diag<float2>(e, bd + (uint64_t)off, zp, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
       }
       out[off] = e;
     }
@@ -314,10 +283,11 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_reg_kernel(const __grid
 
 // ------------------------------------------------------------ backward
 
-// Two CTAs of 256 threads per SM (lambda and psi, 32 registers each, plus the
-// per-thread sums).  When NT > 0 the two tile buffers hold lambda and psi for
-// a round trip; a barrier before each round trip orders it after the last
-// reads of the previous one.
+// NT: 0 (rotations on bits 8..11 only) or 1 (bits 4..7 as well: one round
+// trip L1 -> L3).  Two CTAs of 256 threads per SM (lambda and psi, 32
+// registers each, plus the per-thread sums).  When NT = 1 the two tile
+// buffers hold lambda and psi for the round trip; a barrier before it orders
+// it after the previous tile's reads.
 template <bool UNCOMPUTE, int NT>
 __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid_constant__ SweepDesc d,
                                                                     SweepPtrs<float> p) {
@@ -344,10 +314,10 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
   const bool need_w = d.nz > 0 || d.gslot >= 0;
   const float w0r = (float)d.cost_w0;
   const int mk = rot_mask(d);
-  const int m1 = (mk >> 8) & 15, m2 = mk & 15, m3 = (mk >> 4) & 15;
-  // psi is inverse-rotated in a phase when a later phase reduces against it,
-  // or when it is uncomputed
-  const bool psi1 = UNCOMPUTE || m2 || m3, psi2 = UNCOMPUTE || m3;
+  const int m1 = (mk >> 8) & 15, m3 = (mk >> 4) & 15;
+  // psi is inverse-rotated by the bits 8..11 rotations when the bits 4..7
+  // sums are taken against it, or when it is uncomputed
+  const bool psi1 = UNCOMPUTE || m3;
   // uncomputed psi: see sweep_bwd_kernel (qg_sweep.cu)
   float psi_mult = 1.f;
   if (UNCOMPUTE) {
@@ -368,7 +338,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
   const Parts P3 = make_parts<3>(d);
   const int64_t t3 = deposit(Lay<3>::thr(lane, warp), d.bits, RT);
   const int z3 = zpattern((uint64_t)t3, d);
-  const int s1 = swf(Lay<1>::thr(lane, warp)), s2 = swf(Lay<2>::thr(lane, warp)), s3 = swf(Lay<3>::thr(lane, warp));
+  const int s1 = swf(Lay<1>::thr(lane, warp)), s3 = swf(Lay<3>::thr(lane, warp));
   TileBases tb(S.outside, n - RT, n, d.bits, RT);
 
   float acc[RT];
@@ -387,7 +357,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
     float2 la[RK], qa[RK];
     // load lambda and psi in L1, each gathered through the CNOT ladder when
     // the entangler that follows this sweep is undone on it
-    {
+    if (d.lam_undo == ENT_CNOT || d.psi_undo == ENT_CNOT) {
       const int64_t lb = (int64_t)(ladder_fwd((uint64_t)base, lm) ^ lt1);
 #pragma unroll
       for (int k = 0; k < RK; ++k) {
@@ -398,6 +368,14 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
         const int64_t x = (int64_t)bd + part_off(P1, k);
         la[k] = p.lam_in[d.lam_undo == ENT_CNOT ? s : x];
         qa[k] = p.psi_in[d.psi_undo == ENT_CNOT ? s : x];
+      }
+    } else {
+      const float2* lin = p.lam_in + bd;
+      const float2* pin = p.psi_in + bd;
+#pragma unroll
+      for (int k = 0; k < RK; ++k) {
+        la[k] = lin[part_off(P1, k)];
+        qa[k] = pin[part_off(P1, k)];
       }
     }
     if (d.lam_undo == ENT_CZ || d.psi_undo == ENT_CZ) {
@@ -438,23 +416,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
     red_phase<8>(la, qa, m1, R, acc);
     rot_phase<-1, 8>(la, m1, R);
     if (psi1) rot_phase<-1, 8>(qa, m1, R);
-    if (NT == 2) {
-      if (!first) __syncthreads();
-      to_smem<1>(bl, la, s1);
-      to_smem<1>(bp, qa, s1);
-      __syncthreads();
-      from_smem<2>(bl, la, s2);
-      from_smem<2>(bp, qa, s2);
-      red_phase<0>(la, qa, m2, R, acc);
-      rot_phase<-1, 0>(la, m2, R);
-      if (psi2) rot_phase<-1, 0>(qa, m2, R);
-      __syncthreads();
-      to_smem<2>(bl, la, s2);
-      if (psi2) to_smem<2>(bp, qa, s2);
-      __syncthreads();
-      from_smem<3>(bl, la, s3);
-      if (psi2) from_smem<3>(bp, qa, s3);
-    } else if (NT == 1) {
+    if (NT == 1) {
       if (!first) __syncthreads();
       to_smem<1>(bl, la, s1);
       if (psi1) to_smem<1>(bp, qa, s1);
@@ -492,23 +454,19 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
     }
   }
 
-  // per-thread sums into the warp slots once per CTA; later phases' sums
-  // carry 1/kappa^2 of every rotation already applied to lambda and psi
-  float k1 = 1.f, k12 = 1.f;
+  // per-thread sums into the warp slots once per CTA; the bits 4..7 sums
+  // carry 1/kappa^2 of every bits 8..11 rotation already applied to lambda
+  // and psi
+  float k1 = 1.f;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     if ((m1 >> i) & 1) k1 *= R.kap2[8 + i];
   }
-  k12 = k1;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    if ((m2 >> i) & 1) k12 *= R.kap2[i];
-  }
-#pragma unroll
-  for (int b = 0; b < RT; ++b) {
+  for (int b = 4; b < RT; ++b) {
     const int g = R.gate[b];
     if (g < 0) continue;
-    const float sc = b >= 8 ? 1.f : b < 4 ? k1 : k12;
+    const float sc = b >= 8 ? 1.f : k1;
     const float v = warp_sum(acc[b] * sc);
     if (lane == 0) S.redf[warp][RS_XY + g] += v;
   }
@@ -559,14 +517,25 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
 
 // ------------------------------------------------------------ launchers
 
+// Measured per sweep at n=24 (ncu, GB300): the register layout wins where a
+// sweep needs few round trips -- forward sweeps with none (55 against
+// 59 us), backward sweeps with at most one (82 against 94 us, 109 against
+// 119 us).  With two round trips (the 12 rotations of the low-bit sweep)
+// its unrolled per-bit rotation code outgrows the instruction cache and
+// issue-bound, and the shared-memory kernels (qg_sweep.cu) are faster.
 bool reg_sweep_applies(const SweepDesc& d, bool bwd) {
-  return d.t == RT && (bwd || d.start == START_LOAD);
+  if (d.t != RT) return false;
+  const int nt = reg_transposes(d);
+  return bwd ? nt <= 1 : (d.start == START_LOAD && nt == 0);
 }
 
 int sweep_occupancy_class(const SweepDesc& d) { return d.t == RT ? reg_transposes(d) : 0; }
 
-size_t reg_sweep_smem(const SweepDesc& d) {
-  size_t s = (reg_transposes(d) > 0 ? 2 : 0) * (size_t)RTS * sizeof(float2);
+
+// dynamic shared memory: the two round-trip buffers (backward sweeps that
+// rotate bits 4..7), the Z table and the cost table
+size_t reg_sweep_smem(const SweepDesc& d, bool bwd) {
+  size_t s = (bwd && reg_transposes(d) > 0 ? 2 : 0) * (size_t)RTS * sizeof(float2);
   s += ((size_t)1 << d.nz) * sizeof(float2);
   if (d.cost == COST_INT) s += (size_t)(2 * d.cost_maxabs + 1) * sizeof(float2);
   return s;
@@ -574,22 +543,15 @@ size_t reg_sweep_smem(const SweepDesc& d) {
 
 const void* reg_sweep_fn(const SweepDesc& d, bool bwd, bool uncompute) {
   const int nt = reg_transposes(d);
-  if (!bwd)
-    return nt == 2 ? (const void*)sweep_fwd_reg_kernel<2>
-                   : nt == 1 ? (const void*)sweep_fwd_reg_kernel<1> : (const void*)sweep_fwd_reg_kernel<0>;
-  if (uncompute)
-    return nt == 2 ? (const void*)sweep_bwd_reg_kernel<true, 2>
-                   : nt == 1 ? (const void*)sweep_bwd_reg_kernel<true, 1> : (const void*)sweep_bwd_reg_kernel<true, 0>;
-  return nt == 2 ? (const void*)sweep_bwd_reg_kernel<false, 2>
-                 : nt == 1 ? (const void*)sweep_bwd_reg_kernel<false, 1> : (const void*)sweep_bwd_reg_kernel<false, 0>;
+  if (!bwd) return (const void*)sweep_fwd_reg_kernel;
+  if (uncompute) return nt == 1 ? (const void*)sweep_bwd_reg_kernel<true, 1> : (const void*)sweep_bwd_reg_kernel<true, 0>;
+  return nt == 1 ? (const void*)sweep_bwd_reg_kernel<false, 1> : (const void*)sweep_bwd_reg_kernel<false, 0>;
 }
 
 cudaError_t prepare_reg_sweep_kernels(int optin) {
-  const void* fns[] = {(const void*)sweep_fwd_reg_kernel<0>,        (const void*)sweep_fwd_reg_kernel<1>,
-                       (const void*)sweep_fwd_reg_kernel<2>,        (const void*)sweep_bwd_reg_kernel<false, 0>,
-                       (const void*)sweep_bwd_reg_kernel<false, 1>, (const void*)sweep_bwd_reg_kernel<false, 2>,
-                       (const void*)sweep_bwd_reg_kernel<true, 0>,  (const void*)sweep_bwd_reg_kernel<true, 1>,
-                       (const void*)sweep_bwd_reg_kernel<true, 2>};
+  const void* fns[] = {(const void*)sweep_fwd_reg_kernel, (const void*)sweep_bwd_reg_kernel<false, 0>,
+                       (const void*)sweep_bwd_reg_kernel<false, 1>, (const void*)sweep_bwd_reg_kernel<true, 0>,
+                       (const void*)sweep_bwd_reg_kernel<true, 1>};
   for (const void* fn : fns) {
     cudaFuncAttributes a;
     cudaError_t e = cudaFuncGetAttributes(&a, fn);
@@ -601,27 +563,17 @@ cudaError_t prepare_reg_sweep_kernels(int optin) {
 }
 
 cudaError_t launch_reg_sweep_fwd(const SweepDesc& d, const SweepPtrs<float>& p, int grid, cudaStream_t st, bool pdl) {
-  const size_t smem = reg_sweep_smem(d);
-  switch (reg_transposes(d)) {
-    case 2:
-      return launch_pdl(sweep_fwd_reg_kernel<2>, grid, smem, st, pdl, d, p);
-    case 1:
-      return launch_pdl(sweep_fwd_reg_kernel<1>, grid, smem, st, pdl, d, p);
-    default:
-      return launch_pdl(sweep_fwd_reg_kernel<0>, grid, smem, st, pdl, d, p);
-  }
+  return launch_pdl(sweep_fwd_reg_kernel, grid, reg_sweep_smem(d, false), st, pdl, d, p);
 }
 
 cudaError_t launch_reg_sweep_bwd(const SweepDesc& d, const SweepPtrs<float>& p, bool uncompute, int grid,
                                  cudaStream_t st, bool pdl) {
-  const size_t smem = reg_sweep_smem(d);
+  const size_t smem = reg_sweep_smem(d, true);
   const int nt = reg_transposes(d);
   if (uncompute) {
-    if (nt == 2) return launch_pdl(sweep_bwd_reg_kernel<true, 2>, grid, smem, st, pdl, d, p);
     if (nt == 1) return launch_pdl(sweep_bwd_reg_kernel<true, 1>, grid, smem, st, pdl, d, p);
     return launch_pdl(sweep_bwd_reg_kernel<true, 0>, grid, smem, st, pdl, d, p);
   }
-  if (nt == 2) return launch_pdl(sweep_bwd_reg_kernel<false, 2>, grid, smem, st, pdl, d, p);
   if (nt == 1) return launch_pdl(sweep_bwd_reg_kernel<false, 1>, grid, smem, st, pdl, d, p);
   return launch_pdl(sweep_bwd_reg_kernel<false, 0>, grid, smem, st, pdl, d, p);
 }
