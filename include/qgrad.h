@@ -59,8 +59,16 @@ enum qg_status {
 enum qg_dtype { QG_C128 = 0, QG_C64 = 1 };
 
 /* Entangler of a McClean layer.  QG_ENT_CNOT_LADDER is the reference's
- * ladder (state.py:209-251): CNOT(q, q+1) on odd q, then on even q. */
-enum qg_entangler { QG_ENT_NONE = 0, QG_ENT_CNOT_LADDER = 1, QG_ENT_CZ_LADDER = 2 };
+ * ladder (state.py:209-251): CNOT(q, q+1) on odd q, then on even q.
+ * QG_ENT_CNOT_LADDER_PERIODIC is its periodic form (load_cnot_ladder(
+ * periodic=True), state.py:209-241): CNOT(n-1, 0) joins the odd pairs; even n
+ * only (QG_ERR_INVALID otherwise, where the reference raises ValueError). */
+enum qg_entangler {
+  QG_ENT_NONE = 0,
+  QG_ENT_CNOT_LADDER = 1,
+  QG_ENT_CZ_LADDER = 2,
+  QG_ENT_CNOT_LADDER_PERIODIC = 3
+};
 /* Where the entangler sits in a layer.  The reference applies it before the
  * rotations (mc_clean.py:58-62). */
 enum qg_placement { QG_PLACE_BEFORE = 0, QG_PLACE_AFTER = 1 };
@@ -222,7 +230,8 @@ typedef struct qg_cost_term {
 typedef struct qg_batch_job {
   int32_t kind;        /* 0 McClean, 1 QAOA */
   int32_t n, layers;
-  int32_t entangler;   /* McClean: qg_entangler */
+  int32_t entangler;   /* McClean: qg_entangler (QG_ENT_CNOT_LADDER_PERIODIC only in jobs one
+                          CTA holds: complex64 n <= 13, complex128 n <= 12) */
   int32_t placement;   /* McClean: qg_placement */
   int32_t nterms;      /* observable terms */
   const qg_term* terms;

@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libqg_oracle.so")
 
 X, Y, Z, ZZ = 0, 1, 2, 3
-ENT_NONE, ENT_CNOT, ENT_CZ = 0, 1, 2
+ENT_NONE, ENT_CNOT, ENT_CZ, ENT_CNOT_PERIODIC = 0, 1, 2, 3
 PLACE_BEFORE, PLACE_AFTER = 0, 1
 
 

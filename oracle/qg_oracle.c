@@ -12,7 +12,7 @@
  *   - qradient/physical_components/state.py:142-149 yrot / dyrot
  *   - qradient/physical_components/state.py:168-175 zrot / dzrot
  *   - qradient/physical_components/state.py:209-251 CNOT ladder (odd pairs,
- *     then even pairs; stacking 1 is the inverse)
+ *     then even pairs; stacking 1 is the inverse), open or periodic
  *   - qradient/physical_components/state.py:261-301,319-321 classical
  *     Hamiltonian, exp(-i g C), (-i C)
  *   - qradient/physical_components/state.py:107-123 x_summed = 1/2 sum(-iX)
@@ -45,7 +45,7 @@ static const double QGO_PI = 3.14159265358979323846;
 
 enum { QGO_OK = 0, QGO_EINVAL = 1, QGO_ENOMEM = 2 };
 enum { QGO_X = 0, QGO_Y = 1, QGO_Z = 2, QGO_ZZ = 3 };
-enum { QGO_ENT_NONE = 0, QGO_ENT_CNOT = 1, QGO_ENT_CZ = 2 };
+enum { QGO_ENT_NONE = 0, QGO_ENT_CNOT = 1, QGO_ENT_CZ = 2, QGO_ENT_CNOT_PERIODIC = 3 };
 
 static inline int64_t bitpos(int n, int q) { return (int64_t)(n - 1 - q); }
 
@@ -132,13 +132,18 @@ static void drot(cplx* v, int n, int q, int axis, double angle) {
 /* Basis permutation of the reference CNOT ladder (state.py:229-241): the
  * matrix product puts the odd-pair CNOTs (1,2),(3,4),... rightmost, so they
  * act first, then the even pairs (0,1),(2,3),...  CNOT(c, t) flips bit t when
- * bit c is set.  Returns A(x) with ladder|x> = |A(x)>; stacking 1 applies the
- * inverse (even pairs first, then odd pairs). */
-static int64_t ladder_map(int64_t x, int n, int inverse) {
+ * bit c is set.  The periodic ladder (state.py:218-219,231-232, even n) adds
+ * CNOT(n-1, 0) to the odd pairs.  Returns A(x) with ladder|x> = |A(x)>;
+ * stacking 1 applies the inverse (even pairs first, then odd pairs). */
+static int64_t ladder_map(int64_t x, int n, int inverse, int periodic) {
   for (int pass = 0; pass < 2; pass++) {
     const int first = inverse ? (pass == 0 ? 0 : 1) : (pass == 0 ? 1 : 0);
     for (int c = first; c + 1 < n; c += 2) {
       const int64_t cb = bitpos(n, c), tb = bitpos(n, c + 1);
+      if ((x >> cb) & 1) x ^= (int64_t)1 << tb;
+    }
+    if (periodic && first == 1 && n >= 2) {
+      const int64_t cb = bitpos(n, n - 1), tb = bitpos(n, 0);
       if ((x >> cb) & 1) x ^= (int64_t)1 << tb;
     }
   }
@@ -157,9 +162,11 @@ static int entangle(cplx* v, cplx* scratch, int n, int kind, int inverse) {
     }
     return QGO_OK;
   }
-  if (kind != QGO_ENT_CNOT) return QGO_EINVAL;
+  if (kind != QGO_ENT_CNOT && kind != QGO_ENT_CNOT_PERIODIC) return QGO_EINVAL;
+  const int periodic = kind == QGO_ENT_CNOT_PERIODIC;
+  if (periodic && (n % 2)) return QGO_EINVAL; /* ambiguous for odd n (state.py:210-214) */
 #pragma omp parallel for schedule(static)
-  for (int64_t x = 0; x < N; x++) scratch[ladder_map(x, n, inverse)] = v[x];
+  for (int64_t x = 0; x < N; x++) scratch[ladder_map(x, n, inverse, periodic)] = v[x];
   memcpy(v, scratch, sizeof(cplx) * (size_t)N);
   return QGO_OK;
 }
@@ -228,8 +235,9 @@ static void mcclean_start(cplx* v, int n, const double* ini) {
   for (int q = 0; q < n; q++) rot_xy(v, n, q, QGO_Y, QGO_PI / 4.0);
 }
 
-static int check_mcclean(int n, int L, const int* axes) {
+static int check_mcclean(int n, int L, const int* axes, int entangler) {
   if (n < 1 || n > 34 || L < 0) return QGO_EINVAL;
+  if (entangler < 0 || entangler > 3 || (entangler == QGO_ENT_CNOT_PERIODIC && (n % 2))) return QGO_EINVAL;
   for (int64_t k = 0; k < (int64_t)L * n; k++)
     if (axes[k] < 0 || axes[k] > 2) return QGO_EINVAL; /* mc_clean.py:391-392 */
   return QGO_OK;
@@ -241,7 +249,7 @@ static int check_mcclean(int n, int L, const int* axes) {
 int qgo_mcclean_run(int n, int L, const int* axes, const double* angles, int entangler, int placement, int nterms,
                     const int* kind, const int* q0, const int* q1, const double* w, const double* ini, double* E,
                     double* final_state) {
-  int st = check_mcclean(n, L, axes);
+  int st = check_mcclean(n, L, axes, entangler);
   if (st) return st;
   const int64_t N = (int64_t)1 << n;
   cplx* v = (cplx*)malloc(sizeof(cplx) * (size_t)N);
@@ -341,7 +349,7 @@ static double grad_entry(const cplx* h, const cplx* v, int n, int q, int axis, d
 static int mcclean_grad_impl(int n, int L, const int* axes, const double* angles, int entangler, int placement,
                              int nterms, const int* kind, const int* q0, const int* q1, const double* w,
                              const double* ini, double* E, double* grad, int uncompute) {
-  int st = check_mcclean(n, L, axes);
+  int st = check_mcclean(n, L, axes, entangler);
   if (st) return st;
   const int64_t N = (int64_t)1 << n;
   const size_t nh = uncompute ? 1 : (size_t)(L + 1);

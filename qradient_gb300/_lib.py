@@ -10,7 +10,7 @@ from . import build as _build
 
 QG_OK, QG_ERR_INVALID, QG_ERR_CUDA, QG_ERR_WORKSPACE, QG_ERR_UNSUPPORTED, QG_ERR_HOST_MEMORY = range(6)
 QG_C128, QG_C64 = 0, 1
-QG_ENT_NONE, QG_ENT_CNOT_LADDER, QG_ENT_CZ_LADDER = 0, 1, 2
+QG_ENT_NONE, QG_ENT_CNOT_LADDER, QG_ENT_CZ_LADDER, QG_ENT_CNOT_LADDER_PERIODIC = 0, 1, 2, 3
 QG_PLACE_BEFORE, QG_PLACE_AFTER = 0, 1
 QG_PAULI_X, QG_PAULI_Y, QG_PAULI_Z, QG_PAULI_ZZ = 0, 1, 2, 3
 QG_OP_RUN, QG_OP_GRAD_HISTORY, QG_OP_GRAD_UNCOMPUTE = 0, 1, 2

@@ -30,7 +30,7 @@ _TERM = np.dtype([("kind", "<i4"), ("q0", "<i4"), ("q1", "<i4"), ("pad", "<i4"),
 _COST = np.dtype([("b0", "<i4"), ("b1", "<i4"), ("c", "<i4"), ("pad", "<i4")])
 
 _ENT = {"cnot": _lib.QG_ENT_CNOT_LADDER, "cz": _lib.QG_ENT_CZ_LADDER, None: _lib.QG_ENT_NONE,
-        "none": _lib.QG_ENT_NONE}
+        "none": _lib.QG_ENT_NONE, "cnot_periodic": _lib.QG_ENT_CNOT_LADDER_PERIODIC}
 _PLACE = {"before": _lib.QG_PLACE_BEFORE, "after": _lib.QG_PLACE_AFTER}
 
 # largest qubit count held by one CTA / by a 2-CTA cluster
@@ -134,12 +134,14 @@ class Batch:
         split = max(4, min(self.cluster_from, single + 1))
         # job tables filled column by column (one numpy assignment per field)
         cols = {k: [] for k in ("i", "kind", "n", "layers", "entangler", "placement", "nterms", "terms", "axes",
-                                "cost_nterms", "cost_maxabs", "cost_w0", "cost")}
+                                "cost_nterms", "cost_maxabs", "cost_w0", "cost", "periodic")}
         big = []
         for i, s in enumerate(self._specs):
             c = s["circuit"]
             st = cache[id(c)]
-            if c.qnum > cmax or st is None:
+            # the periodic ladder targets the top qubit, which a 2-CTA job splits
+            periodic = s["kind"] == 0 and c.entangler == "cnot_periodic"
+            if c.qnum > cmax or st is None or (periodic and c.qnum > single):
                 big.append(i)
                 continue
             mc = s["kind"] == 0
@@ -147,14 +149,15 @@ class Batch:
                          ("entangler", _ENT[c.entangler] if mc else 0), ("placement", _PLACE[c.placement] if mc else 0),
                          ("nterms", st["nterms"]), ("terms", st["terms"]), ("axes", st["axes"]),
                          ("cost_nterms", st["cost_nterms"]), ("cost_maxabs", st["cost_maxabs"]),
-                         ("cost_w0", st["cost_w0"]), ("cost", st["cost"])):
+                         ("cost_w0", st["cost_w0"]), ("cost", st["cost"]), ("periodic", periodic)):
                 cols[k].append(v)
         idx = np.asarray(cols["i"], dtype=np.int64)
         qn = np.asarray(cols["n"], dtype=np.int64)
         offs = np.asarray([self._specs[i]["off"] for i in idx], dtype=np.uint64)
         pbase, gbase, ebase = self.params_flat.data_ptr(), self.grads_flat.data_ptr(), self.expec.data_ptr()
         self._groups = []
-        for cl, sel in ((1, qn < split), (2, qn >= split)):
+        per = np.asarray(cols["periodic"], dtype=bool)
+        for cl, sel in ((1, (qn < split) | per), (2, (qn >= split) & ~per)):
             nj = int(sel.sum())
             if nj == 0:
                 continue

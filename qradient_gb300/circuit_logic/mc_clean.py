@@ -11,7 +11,9 @@ starts from Ry(pi/4) on every qubit of |0..0> (or of ``ini_state``).
 
 Extra keyword arguments (not in the reference):
   entangler  'cnot' (default: the reference's CNOT ladder, state.py:209-251),
-             'cz' (CZ on neighbours) or None
+             'cnot_periodic' (its periodic form, load_cnot_ladder(periodic=True):
+             CNOT(n-1, 0) joins the odd pairs; even n only), 'cz' (CZ on
+             neighbours) or None
   placement  'before' (default, as the reference) or 'after' the rotations
   dtype, device, grad_mode  see ParametrizedCircuit
 """
@@ -22,7 +24,7 @@ from .. import _lib, _native
 from .base import ParametrizedCircuit
 
 _ENT = {"cnot": _lib.QG_ENT_CNOT_LADDER, "cz": _lib.QG_ENT_CZ_LADDER, None: _lib.QG_ENT_NONE,
-        "none": _lib.QG_ENT_NONE}
+        "none": _lib.QG_ENT_NONE, "cnot_periodic": _lib.QG_ENT_CNOT_LADDER_PERIODIC}
 _PLACE = {"before": _lib.QG_PLACE_BEFORE, "after": _lib.QG_PLACE_AFTER}
 
 
@@ -39,7 +41,11 @@ class McClean(ParametrizedCircuit):
         self.angles = kwargs.get("angles", default_angles)
         ent = kwargs.get("entangler", "cnot")
         if ent not in _ENT:
-            raise ValueError("entangler must be 'cnot', 'cz' or None")
+            raise ValueError("entangler must be 'cnot', 'cnot_periodic', 'cz' or None")
+        if ent == "cnot_periodic" and self.qnum % 2:
+            # state.py:210-214
+            raise ValueError(("CNOT gates in a ladder structure with periodic boundaries",
+                              "are ambiguous for uneven number of qubits."))
         self.entangler = ent
         placement = kwargs.get("placement", "before")
         if placement not in _PLACE:

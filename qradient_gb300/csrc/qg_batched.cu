@@ -47,15 +47,18 @@ __device__ __forceinline__ void sincosT(float a, float* s, float* c) { sincosf(a
 __device__ __forceinline__ int swb(int e, bool dbl) { return dbl ? e ^ ((e >> 3) & 7) : e ^ ((e >> 4) & 15); }
 __device__ __forceinline__ int ins0(int p, int j) { return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1)); }
 
-// index arithmetic of the batched kernel is 32-bit: its jobs have at most 26 qubits
-__device__ __forceinline__ uint32_t lad_fwd(uint32_t x, uint32_t odd, uint32_t even) {
-  x ^= (x & odd) >> 1;
+// index arithmetic of the batched kernel is 32-bit: its jobs have at most 26
+// qubits.  The periodic ladder adds CNOT(n-1, 0) to the odd pairs: bit n-1
+// flips when bit 0 is set (wrap = 1, wshift = n - 1; wrap = 0 for the open
+// ladder).  It targets the top bit, so periodic jobs run in one CTA only.
+__device__ __forceinline__ uint32_t lad_fwd(uint32_t x, uint32_t odd, uint32_t even, uint32_t wrap, int wshift) {
+  x ^= ((x & odd) >> 1) ^ ((x & wrap) << wshift);
   x ^= (x & even) >> 1;
   return x;
 }
-__device__ __forceinline__ uint32_t lad_inv(uint32_t x, uint32_t odd, uint32_t even) {
+__device__ __forceinline__ uint32_t lad_inv(uint32_t x, uint32_t odd, uint32_t even, uint32_t wrap, int wshift) {
   x ^= (x & even) >> 1;
-  x ^= (x & odd) >> 1;
+  x ^= ((x & odd) >> 1) ^ ((x & wrap) << wshift);
   return x;
 }
 
@@ -412,6 +415,8 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     const bool grad = J.grad != nullptr;
     const int L = J.layers;
     uint32_t lodd = 0, leven = 0;
+    const uint32_t lwrap = J.entangler == 3 ? 1u : 0u;
+    const int lws = n - 1;
     for (int q = 0; q + 1 < n; ++q) {
       const uint32_t b = 1u << (n - 1 - q);
       if (q & 1)
@@ -567,7 +572,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       if (J.kind == 0 && tid < (M + NT - 1) / NT) {
         int pat = 0, patf = 0;
         const uint32_t xk = top | (uint32_t)(tid * NT);
-        const uint32_t xf = lad_fwd(xk, lodd, leven);
+        const uint32_t xf = lad_fwd(xk, lodd, leven, lwrap, lws);
         for (int j = 0; j < nzt; ++j) {
           pat |= (int)((xk >> S.zbit[j]) & 1) << j;
           patf |= (int)((xf >> S.zbit[j]) & 1) << j;
@@ -630,7 +635,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       }
       for (int e = tid; e < M; e += NT) {
         const uint32_t x = top | (uint32_t)e;
-        const uint32_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
+        const uint32_t src = inv ? lad_fwd(x, lodd, leven, lwrap, lws) : lad_inv(x, lodd, leven, lwrap, lws);
         scr[swb(e, DBL)] = v[swb((int)(src & (uint32_t)(M - 1)), DBL)];
       }
       __syncthreads();
@@ -718,7 +723,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     auto entangle_diag = [&](C*& v, bool inv) {
       const int nzt = S.nz;  // callers fuse only when every Z rotation is in the table
       int ptid = 0;
-      const uint32_t tsrc = (inv && J.entangler == 1) ? lad_fwd((uint32_t)tid, lodd, leven) : (uint32_t)tid;
+      const uint32_t tsrc = (inv && (J.entangler == 1 || J.entangler == 3)) ? lad_fwd((uint32_t)tid, lodd, leven, lwrap, lws) : (uint32_t)tid;
       for (int j = 0; j < nzt; ++j) ptid |= (int)((tsrc >> S.zbit[j]) & 1) << j;
       if (J.entangler == 2) {
         // CZ: a sign, its own inverse, in place
@@ -736,7 +741,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       }
       for (int e = tid, k = 0; e < M; e += NT, ++k) {
         const uint32_t x = top | (uint32_t)e;
-        const uint32_t src = inv ? lad_fwd(x, lodd, leven) : lad_inv(x, lodd, leven);
+        const uint32_t src = inv ? lad_fwd(x, lodd, leven, lwrap, lws) : lad_inv(x, lodd, leven, lwrap, lws);
         const int pat = inv ? (ptid ^ S.zpkf[k]) : (ptid | S.zpk[k]);
         scr[swb(e, DBL)] = cmulb(v[swb((int)(src & (uint32_t)(M - 1)), DBL)], ztab[pat]);
       }

@@ -263,6 +263,7 @@ struct Program {
   Layout lay;
   std::vector<SweepDesc> sweeps;
   int8_t obs_pre = ENT_NONE;  // entangler between the last sweep and the observable
+  int8_t periodic = 0;        // the CNOT ladder is the periodic one
   int first_param = 0;   // first sweep with gradient slots
   int nslots = 0;        // gradient slots (before the expectation slots)
   int grad_kind = 0;     // finalize layout
@@ -285,9 +286,9 @@ int build_program(const qg_circuit* c, int dtype, bool with_ini, Program& P) {
       if (st) return st;
     }
     P.first_param = (int)P.sweeps.size();
-    const int8_t e = c->entangler == QG_ENT_CNOT_LADDER ? ENT_CNOT
-                     : c->entangler == QG_ENT_CZ_LADDER ? ENT_CZ
-                                                        : ENT_NONE;
+    const int8_t e = (c->entangler == QG_ENT_CNOT_LADDER || c->entangler == QG_ENT_CNOT_LADDER_PERIODIC) ? ENT_CNOT
+                     : c->entangler == QG_ENT_CZ_LADDER                                          ? ENT_CZ
+                                                                                                 : ENT_NONE;
     for (int i = 0; i < c->L; ++i) {
       std::vector<LayerGate> g(n);
       for (int q = 0; q < n; ++q) g[q] = LayerGate{c->axes[i * n + q], angle_param(i * n + q), i * n + q};
@@ -330,7 +331,11 @@ int build_program(const qg_circuit* c, int dtype, bool with_ini, Program& P) {
     P.sweeps.push_back(blank_sweep(n, P.lay.tiles[0]));
     P.first_param = 1;
   }
-  for (auto& d : P.sweeps) d.start = START_LOAD;
+  P.periodic = c->kind == 0 && c->entangler == QG_ENT_CNOT_LADDER_PERIODIC;
+  for (auto& d : P.sweeps) {
+    d.start = START_LOAD;
+    d.periodic = P.periodic;
+  }
   if (!with_ini) P.sweeps[0].start = c->kind == 0 ? START_MCCLEAN : START_PLUS;
   return QG_OK;
 }
@@ -573,6 +578,7 @@ std::vector<ObsDesc> build_obs(const qg_circuit* c, const Program& P, bool grad,
     for (size_t i = 0; i < lay.tiles[s].size(); ++i) d->bits[i] = (uint8_t)lay.tiles[s][i];
     d->store = store;
     d->pre = P.obs_pre;
+    d->periodic = P.periodic;
     return d;
   };
   if (c->kind == 1 && grad) {
@@ -856,7 +862,11 @@ int qg_mcclean_create(int n, int layers, const int32_t* axes, int entangler, int
   if (n < 1 || n > QMAX) return fail(QG_ERR_UNSUPPORTED, "qubit number %d outside 1..%d", n, QMAX);
   if (layers < 0) return fail(QG_ERR_INVALID, "negative layer number");
   if (layers > 0 && !axes) return fail(QG_ERR_INVALID, "null axes");
-  if (entangler < 0 || entangler > 2) return fail(QG_ERR_INVALID, "unknown entangler %d", entangler);
+  if (entangler < 0 || entangler > 3) return fail(QG_ERR_INVALID, "unknown entangler %d", entangler);
+  if (entangler == QG_ENT_CNOT_LADDER_PERIODIC && n % 2)
+    return fail(QG_ERR_INVALID,
+                "CNOT gates in a ladder structure with periodic boundaries are ambiguous for uneven number of "
+                "qubits.");  // state.py:210-214
   if (placement < 0 || placement > 1) return fail(QG_ERR_INVALID, "unknown placement %d", placement);
   qg_circuit* c = new (std::nothrow) qg_circuit;
   if (!c) return fail(QG_ERR_HOST_MEMORY, "host allocation failed");

@@ -39,7 +39,8 @@ enum Axis : int8_t { AX_X = 0, AX_Y = 1, AX_Z = 2 };
 // other than the one it writes); the CZ ladder is a sign and works in place.
 enum Ent : int8_t {
   ENT_NONE = 0,
-  ENT_CNOT = 1,  // reference CNOT ladder, state.py:209-251 (odd pairs, then even pairs)
+  ENT_CNOT = 1,  // reference CNOT ladder, state.py:209-251 (odd pairs, then even pairs; open or,
+                 // with the descriptor's periodic flag, periodic)
   ENT_CZ = 2,    // CZ on neighbours (q, q+1)
 };
 
@@ -94,7 +95,7 @@ struct SweepDesc {
   int8_t cost;             // CostKind: QAOA exp(-i gamma C), applied before the gates
   int8_t psi_undo;         // backward: Ent undone on psi as it is loaded (uncompute mode)
   int8_t gcost;            // CostKind of the gslot reduction
-  int8_t pad;
+  int8_t periodic;         // the CNOT ladder is the periodic one (CNOT(n-1, 0) joins the odd pairs)
   AngleRef cost_angle;     // gamma
   int32_t cost_maxabs;     // |m| <= cost_maxabs (COST_INT)
   int32_t gslot;           // backward: slot of Im<lam|C|psi> at the load point, -1 if none
@@ -123,7 +124,8 @@ struct ObsDesc {
   int8_t store;        // write lam
   int8_t cost;         // diagonal from the QAOA cost (CostKind) instead of the diagonal terms
   int8_t pre;          // Ent applied to psi as it is loaded (entangler after the last layer)
-  int8_t pad0[3];
+  int8_t periodic;     // ENT_CNOT is the periodic ladder
+  int8_t pad0[2];
   int32_t ndiag;       // diagonal terms (first)
   int32_t nxy;         // X/Y terms handled here (after the diagonal ones)
   int32_t eslot;       // slot of the expectation partial sums

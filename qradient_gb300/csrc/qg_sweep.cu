@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(NTHREADS) sweep_fwd_kernel(const __grid_consta
   pdl_wait();
 
   const int tid = threadIdx.x;
-  const LadderMasks lm = ladder_masks(n);
+  const LadderMasks lm = ladder_masks(n, d.periodic);
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
   pdl_wait();
 
   const int tid = threadIdx.x;
-  const LadderMasks lm = ladder_masks(n);
+  const LadderMasks lm = ladder_masks(n, d.periodic);
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   pdl_wait();
 
   const int tid = threadIdx.x;
-  const LadderMasks lm = ladder_masks(n);
+  const LadderMasks lm = ladder_masks(n, d.periodic);
   const int nk = tsize > NTHREADS ? tsize / NTHREADS : 1;
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
@@ -891,7 +891,7 @@ __global__ void __launch_bounds__(NTHREADS) observable_kernel(const __grid_const
   const bool active = tid < tsize;
   const int64_t dep_lo = active ? deposit(tid, d.bits, t < 8 ? t : 8) : 0;
   const int64_t ntiles = (int64_t)1 << (n - t);
-  const LadderMasks lm = ladder_masks(n);
+  const LadderMasks lm = ladder_masks(n, d.periodic);
   TileBases tb(outside, n - t, n, d.bits, t);
   const int stid = sw<R>(tid);
   double eacc = 0.0;

@@ -58,13 +58,16 @@ __device__ __forceinline__ double angle_of(const AngleRef& a, const double* para
 // Reference CNOT ladder as a basis permutation: CNOT(q, q+1) flips bit
 // (n-2-q) when bit (n-1-q) is set, i.e. x ^= (x & bit_c) >> 1.  The odd-pair
 // CNOTs act first, then the even pairs (state.py:235-241).  The pairs of one
-// parity are disjoint, so each parity is one masked shift-xor.
+// parity are disjoint, so each parity is one masked shift-xor.  The periodic
+// ladder (state.py:218-219, even n) adds CNOT(n-1, 0) to the odd pairs: bit
+// n-1 flips when bit 0 is set, x ^= (x & wrap) << (n - 1).
 struct LadderMasks {
-  uint64_t odd, even;
+  uint64_t odd, even, wrap;
+  int wshift;
 };
 
-__device__ __forceinline__ LadderMasks ladder_masks(int n) {
-  LadderMasks m{0, 0};
+__device__ __forceinline__ LadderMasks ladder_masks(int n, bool periodic) {
+  LadderMasks m{0, 0, periodic ? 1ull : 0ull, n - 1};
   for (int q = 0; q + 1 < n; ++q) {
     const uint64_t b = 1ull << (n - 1 - q);
     if (q & 1)
@@ -77,14 +80,14 @@ __device__ __forceinline__ LadderMasks ladder_masks(int n) {
 
 // A(x): ladder |x> = |A(x)>
 __device__ __forceinline__ uint64_t ladder_fwd(uint64_t x, const LadderMasks& m) {
-  x ^= (x & m.odd) >> 1;
+  x ^= ((x & m.odd) >> 1) ^ ((x & m.wrap) << m.wshift);
   x ^= (x & m.even) >> 1;
   return x;
 }
 // A^{-1}(x)
 __device__ __forceinline__ uint64_t ladder_inv(uint64_t x, const LadderMasks& m) {
   x ^= (x & m.even) >> 1;
-  x ^= (x & m.odd) >> 1;
+  x ^= ((x & m.odd) >> 1) ^ ((x & m.wrap) << m.wshift);
   return x;
 }
 
@@ -342,7 +345,7 @@ __device__ void sweep_setup(const SweepDesc& d, const double* params, SetupShare
   }
   for (int i = tid; i < (NTHREADS / 32) * RS_N; i += NTHREADS) (&S.red[0][0])[i] = 0.0;  // clears both views
   if (t > 8) {
-    const LadderMasks lm = ladder_masks(n);
+    const LadderMasks lm = ladder_masks(n, d.periodic);
     for (int k = tid; k < (1 << (t - 8)); k += NTHREADS) {
       S.offhi[k] = deposit((int64_t)k << 8, d.bits, t);
       S.zpk[k] = zpattern((uint64_t)S.offhi[k], d);

@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_reg_kernel(const __grid
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = d.n;
-  const LadderMasks lm = ladder_masks(n);
+  const LadderMasks lm = ladder_masks(n, d.periodic);
   const int64_t ntiles = (int64_t)1 << (n - RT);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) sweep_bwd_reg_kernel(const __grid
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = d.n;
-  const LadderMasks lm = ladder_masks(n);
+  const LadderMasks lm = ladder_masks(n, d.periodic);
   const int64_t ntiles = (int64_t)1 << (n - RT);
   const bool fold = d.cost == COST_INT && d.has_diag && d.nz == 0;
   const double gamma = d.cost == COST_REAL ? angle_of(d.cost_angle, p.params) : 0.0;

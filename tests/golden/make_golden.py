@@ -11,6 +11,7 @@ stored beside the outputs, so the tests never need the reference.
 Usage:  python tests/golden/make_golden.py --reference PATH [--big]
         python tests/golden/make_golden.py --optimizer --reference PATH
         python tests/golden/make_golden.py --projectors --reference PATH
+        python tests/golden/make_golden.py --ladder --reference PATH
 
 ``--big`` adds the McClean ZZ-chain cases at n = 18, 20 (L = 50), which take
 about two minutes of reference time.
@@ -300,6 +301,39 @@ def projectors_main(reference):
     print("wrote", len(out), "arrays to projectors.npz")
 
 
+def ladder_main(reference):
+    """The reference's CNOT ladders, periodic and open, as they act on seeded
+    random states: State.load_cnot_ladder(periodic) (state.py:209-241) built
+    by the reference's own State class and applied through its stored
+    matrices (the method cnot_ladder shadows them, state.py:243-251, so they
+    are read as State._State__cnot_ladder).  McClean builds only the open
+    ladder; the periodic one is the reference's other ladder option."""
+    spec = importlib.util.spec_from_file_location(
+        "ref_state", os.path.join(reference, "qradient", "physical_components", "state.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    out = {}
+    rng = np.random.default_rng(2024)
+    for n in (2, 4, 6, 8, 10):
+        st = mod.State(n)
+        for periodic in (True, False):
+            st.load_cnot_ladder(periodic=periodic)
+            mats = st._State__cnot_ladder
+            v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+            tag = "n%d/%s/" % (n, "periodic" if periodic else "open")
+            out[tag + "in"] = v
+            out[tag + "stack0"] = mats[0].dot(v)
+            out[tag + "stack1"] = mats[1].dot(v)
+        print("ladder n=%d" % n, flush=True)
+    try:
+        mod.State(5).load_cnot_ladder(periodic=True)
+        out["odd_n_raises"] = np.array(False)
+    except ValueError:
+        out["odd_n_raises"] = np.array(True)
+    np.savez_compressed(os.path.join(HERE, "ladder.npz"), **out)
+    print("wrote", len(out), "arrays to ladder.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("QRADIENT_REFERENCE"),
@@ -307,11 +341,14 @@ def main():
     ap.add_argument("--big", action="store_true")
     ap.add_argument("--optimizer", action="store_true")
     ap.add_argument("--projectors", action="store_true")
+    ap.add_argument("--ladder", action="store_true")
     args = ap.parse_args()
     if not args.reference:
         ap.error("--reference PATH (or QRADIENT_REFERENCE) is required")
     if args.projectors:
         return projectors_main(args.reference)
+    if args.ladder:
+        return ladder_main(args.reference)
     if args.optimizer:
         return optimizer_main(args.reference)
     McClean, Qaoa = load_reference(args.reference)

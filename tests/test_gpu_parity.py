@@ -185,3 +185,67 @@ def test_invalid_inputs_raise_value_error():
     q = Qaoa(4, {"zz": zz}, 2)
     with pytest.raises(ValueError):
         q.grad_run(np.zeros(3), np.zeros(2))
+
+
+def test_mcclean_periodic_ladder_vs_oracle():
+    """The periodic CNOT ladder (state.py:209-241, periodic=True; its
+    permutation is pinned to the reference's own ladder matrices by
+    test_oracle_golden.py) through the sweep path, both placements and
+    gradient modes, against the oracle; complex64 error stated."""
+    from qradient_gb300 import McClean
+
+    for n, L in ((6, 3), (12, 4), (14, 5), (18, 4)):
+        rng = np.random.default_rng(n)
+        axes = rng.integers(0, 3, (L, n))
+        angles = rng.uniform(0, 2 * np.pi, (L, n))
+        zz = np.full((n, n), None)
+        for i in range(n - 1):
+            zz[i, i + 1] = 1.0
+        x = np.full(n, None)
+        x[n // 2] = 0.6
+        obs = {"zz": zz, "x": x}
+        t = O.Terms.from_dict(n, obs)
+        for place in ("before", "after"):
+            E0, g0 = O.mcclean_grad(n, axes, angles, t, entangler=O.ENT_CNOT_PERIODIC,
+                                    placement=O.PLACE_BEFORE if place == "before" else O.PLACE_AFTER)
+            for mode in ("history", "uncompute"):
+                c = McClean(n, obs, L, axes=axes, angles=angles, entangler="cnot_periodic", placement=place,
+                            grad_mode=mode)
+                E, g = c.grad_run()
+                assert abs(E - E0) <= TOL128 and rel_err(g, g0) <= TOL128, (n, place, mode, rel_err(g, g0))
+                assert abs(c.run_expec_val() - E0) <= TOL128
+            c64 = McClean(n, obs, L, axes=axes, angles=angles, entangler="cnot_periodic", placement=place,
+                          dtype="complex64")
+            E, g = c64.grad_run()
+            assert abs(E - E0) <= TOL64 and rel_err(g, g0) <= TOL64, (n, place, rel_err(g, g0))
+    with pytest.raises(ValueError):
+        McClean(5, {"zz": np.full((5, 5), None)}, 1, entangler="cnot_periodic")
+
+
+def test_batched_periodic_ladder_vs_oracle():
+    """Batched jobs with the periodic ladder: one CTA holds n <= 13
+    (complex64); n = 14 runs on the sweep path inside the same graph (the
+    ladder's CNOT(n-1, 0) targets the qubit a 2-CTA job splits)."""
+    import torch
+
+    from qradient_gb300 import McClean
+    from qradient_gb300.batched import Batch
+
+    b = Batch(dtype="complex64")
+    jobs = []
+    for n, L in ((10, 4), (14, 3), (8, 2)):
+        rng = np.random.default_rng(100 + n)
+        axes = rng.integers(0, 3, (L, n))
+        angles = rng.uniform(0, 2 * np.pi, (L, n))
+        zz = np.full((n, n), None)
+        for i in range(n - 1):
+            zz[i, i + 1] = 1.0
+        c = McClean(n, {"zz": zz}, L, axes=axes, angles=angles, entangler="cnot_periodic", dtype="complex64")
+        jobs.append((b.add(c), n, axes, angles, O.Terms.from_dict(n, {"zz": zz})))
+    b.finalize()
+    E, grads = b.grad()
+    torch.cuda.synchronize()
+    for slot, n, axes, angles, t in jobs:
+        E0, g0 = O.mcclean_grad(n, axes, angles, t, entangler=O.ENT_CNOT_PERIODIC)
+        assert abs(E[slot].item() - E0) <= TOL64, n
+        assert rel_err(grads[slot].cpu().numpy().reshape(g0.shape), g0) <= TOL64, n

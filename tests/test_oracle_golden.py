@@ -125,3 +125,39 @@ def test_uncompute_mode_matches_history_and_reference(golden):
         E, g = O.qaoa_grad(m["n"], c["betas"], c["gammas"], _terms(c), ini=c.get("ini"), uncompute=True)
         assert abs(E - float(c["e_grad"])) <= TOL * max(1.0, abs(float(c["e_grad"]))), m["name"]
         assert rel_err(g, c["grad"]) <= TOL, (m["name"], rel_err(g, c["grad"]))
+
+
+def test_ladders_match_reference():
+    """The oracle's open and periodic CNOT ladders, and their inverses,
+    against the reference's own ladder matrices (State.load_cnot_ladder,
+    state.py:209-241) applied to seeded random states."""
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ladder.npz"))
+    assert bool(z["odd_n_raises"])
+    for n in (2, 4, 6, 8, 10):
+        for kind, ent in (("open", O.ENT_CNOT), ("periodic", O.ENT_CNOT_PERIODIC)):
+            tag = "n%d/%s/" % (n, kind)
+            v = z[tag + "in"]
+            assert np.array_equal(O.entangle(n, v, ent), z[tag + "stack0"]), tag
+            assert np.array_equal(O.entangle(n, v, ent, inverse=True), z[tag + "stack1"]), tag
+    with pytest.raises(ValueError):
+        O.entangle(5, np.ones(32), O.ENT_CNOT_PERIODIC)
+
+
+def test_periodic_ladder_gradient_against_finite_differences():
+    n, L = 6, 3
+    rng = np.random.default_rng(17)
+    axes = rng.integers(0, 3, (L, n))
+    angles = rng.uniform(0, 2 * np.pi, (L, n))
+    t = O.Terms([3, 3, 0], [0, 2, 5], [1, 5, 5], [1.0, 0.7, 0.4])
+    for place in (O.PLACE_BEFORE, O.PLACE_AFTER):
+        _, g = O.mcclean_grad(n, axes, angles, t, entangler=O.ENT_CNOT_PERIODIC, placement=place)
+        h = 1e-5
+        for i, q in ((0, 0), (1, 5), (2, 3)):
+            a = angles.copy()
+            a[i, q] += h
+            ep = O.mcclean_run(n, axes, a, t, entangler=O.ENT_CNOT_PERIODIC, placement=place)
+            a[i, q] -= 2 * h
+            em = O.mcclean_run(n, axes, a, t, entangler=O.ENT_CNOT_PERIODIC, placement=place)
+            assert abs((ep - em) / (2 * h) - g[i, q]) < 1e-8
