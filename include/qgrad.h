@@ -243,6 +243,8 @@ typedef struct qg_batch_job {
   int32_t cost_maxabs;
   double cost_w0;
   const qg_cost_term* cost;
+  double* term_expec;  /* out, optional (NULL: none): <P_k> of every observable term on the final
+                          state, nterms doubles -- what the projector-shot estimators draw from */
 } qg_batch_job;
 
 /* QAOA integer cost of a term list (host): fills up to max_out cost terms,

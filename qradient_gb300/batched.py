@@ -24,8 +24,8 @@ from . import _lib, _native
 _JOB = np.dtype([("kind", "<i4"), ("n", "<i4"), ("layers", "<i4"), ("entangler", "<i4"), ("placement", "<i4"),
                  ("nterms", "<i4"), ("terms", "<u8"), ("axes", "<u8"), ("params", "<u8"), ("expec", "<u8"),
                  ("grad", "<u8"), ("cost_nterms", "<i4"), ("cost_maxabs", "<i4"), ("cost_w0", "<f8"),
-                 ("cost", "<u8")])
-assert _JOB.itemsize == 88
+                 ("cost", "<u8"), ("term_expec", "<u8")])
+assert _JOB.itemsize == 96
 _TERM = np.dtype([("kind", "<i4"), ("q0", "<i4"), ("q1", "<i4"), ("pad", "<i4"), ("w", "<f8")])
 _COST = np.dtype([("b0", "<i4"), ("b1", "<i4"), ("c", "<i4"), ("pad", "<i4")])
 
@@ -55,13 +55,17 @@ def _dev_bytes(arr, device):
 class Batch:
     """A fixed list of jobs executed together; parameters live in ``params``."""
 
-    def __init__(self, device=None, dtype="complex64", grad=True, use_graph=True, cluster_from=None):
+    def __init__(self, device=None, dtype="complex64", grad=True, use_graph=True, cluster_from=None,
+                 term_expectations=False):
         """cluster_from: smallest qubit count whose jobs are split over a
         2-CTA cluster (default: only jobs too large for one CTA);
-        ``tuning.tune_batch`` picks it by timing."""
+        ``tuning.tune_batch`` picks it by timing.  term_expectations: also
+        return <P_k> of every observable term of each job's final state
+        (``term_expec[slot]``, for projector-shot estimates)."""
         self.device = _native.require_cuda(device)
         self.dtype = _native.dtype_code(dtype)
         self.want_grad = grad
+        self.want_terms = term_expectations
         self.use_graph = use_graph
         self.cluster_from = SINGLE_MAX[self.dtype] + 1 if cluster_from is None else int(cluster_from)
         self._specs = []
@@ -111,6 +115,14 @@ class Batch:
         self.expec = torch.empty(max(B, 1), dtype=torch.float64, device=dev)
         self.params = [self.params_flat[s["off"]: s["off"] + s["nparams"]] for s in self._specs]
         self.grads = [self.grads_flat[s["off"]: s["off"] + s["nparams"]] for s in self._specs]
+        toff = 0
+        for s in self._specs:
+            s["toff"] = toff
+            toff += s["circuit"].observable.num_components if self.want_terms else 0
+        self.term_expec_flat = torch.empty(max(toff, 1), dtype=torch.float64, device=dev)
+        self.term_expec = [self.term_expec_flat[s["toff"]: s["toff"] + (s["circuit"].observable.num_components
+                                                                         if self.want_terms else 0)]
+                           for s in self._specs]
         self._structures = {}
         self._build_groups()
         self.finalized = True
@@ -154,7 +166,9 @@ class Batch:
         idx = np.asarray(cols["i"], dtype=np.int64)
         qn = np.asarray(cols["n"], dtype=np.int64)
         offs = np.asarray([self._specs[i]["off"] for i in idx], dtype=np.uint64)
+        toffs = np.asarray([self._specs[i]["toff"] for i in idx], dtype=np.uint64)
         pbase, gbase, ebase = self.params_flat.data_ptr(), self.grads_flat.data_ptr(), self.expec.data_ptr()
+        tbase = self.term_expec_flat.data_ptr()
         self._groups = []
         per = np.asarray(cols["periodic"], dtype=bool)
         for cl, sel in ((1, (qn < split) | per), (2, (qn >= split) & ~per)):
@@ -168,6 +182,7 @@ class Batch:
             arr["params"] = pbase + 8 * offs[sel]
             arr["expec"] = ebase + 8 * idx[sel].astype(np.uint64)
             arr["grad"] = gbase + 8 * offs[sel] if self.want_grad else 0
+            arr["term_expec"] = tbase + 8 * toffs[sel] if self.want_terms else 0
             maxq = int(qn[sel].max())
             ws = torch.empty(256, dtype=torch.uint8, device=dev)  # job counter, cleared by qg_batch_launch
             self._groups.append((cl, _dev_bytes(arr, dev), nj, maxq, ws))
@@ -250,9 +265,14 @@ class Batch:
                 op = _lib.QG_OP_GRAD_UNCOMPUTE
                 e, g = nat.grad(self.params[i], self.dtype, self.device, op,
                                 out=(self.expec[i:i + 1], self.grads[i]))
+                if self.want_terms and self.term_expec[i].numel():
+                    _, st = nat.run(self.params[i], self.dtype, self.device, want_state=True)
+                    nat.pauli_expectations_into(st, self.dtype, self.device, self.term_expec[i])
             else:
-                e, _ = nat.run(self.params[i], self.dtype, self.device)
+                e, st = nat.run(self.params[i], self.dtype, self.device, want_state=self.want_terms)
                 self.expec[i:i + 1].copy_(e)
+                if self.want_terms and self.term_expec[i].numel():
+                    nat.pauli_expectations_into(st, self.dtype, self.device, self.term_expec[i])
 
     def _prepare_big(self):
         # allocate the sweep-path workspaces outside any graph capture

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqgrad.so")
-SOURCES = ["qg_sweep.cu", "qg_sweep_reg.cu", "qg_extra.cu", "qg_capi.cu", "qg_batched.cu", "qg_noalloc.cu", "qg_optim.cu", "qg_shots.cu"]
+SOURCES = ["qg_sweep.cu", "qg_extra.cu", "qg_capi.cu", "qg_batched.cu", "qg_noalloc.cu", "qg_optim.cu", "qg_shots.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -147,8 +147,10 @@ class McClean(ParametrizedCircuit):
         rotating qubit q of layer i by a further +-pi/2.  All rotations of a
         layer commute, so that state is the full circuit with angle
         angles[i, q] +- pi/2; the 2 L n shifted circuits run as forward
-        passes on the device, each followed by one per-term expectation
-        reduction, and one projector-shot launch draws every estimate.
+        passes on the device -- in one batched launch when the circuit fits
+        the shared-memory kernel (complex64 n <= 14, complex128 n <= 13),
+        else one sweep-path run each -- with every term's <P_k> on the final
+        state, and one projector-shot launch draws every estimate.
         shot_num=None gives the exact parameter-shift gradient (infinitely
         many shots).  Shots are Philox draws keyed by `seed` (default: drawn
         from numpy's global RNG)."""
@@ -180,16 +182,32 @@ class McClean(ParametrizedCircuit):
         idx = torch.arange(L * n, device=dev)
         shifted[2 * idx, idx] += np.pi / 2
         shifted[2 * idx + 1, idx] -= np.pi / 2
-        ini = nat.state_tensor(ini_state, dt, dev)
-        ws = nat.workspace(dt, _lib.QG_OP_RUN, dev)
-        energies = torch.empty(rows, dtype=torch.float64, device=dev)
-        state = torch.empty(2 ** n, dtype=_native.torch_dtype(dt), device=dev)
-        expec = torch.empty((rows, max(K, 1)), dtype=torch.float64, device=dev)
         need_terms = shot_num is not None or component_sampling
-        for r in range(rows):
-            nat.run_into(shifted[r], dt, dev, ini, ws, energies[r:r + 1], state if need_terms else None)
+        expec = torch.empty((rows, max(K, 1)), dtype=torch.float64, device=dev)
+        from ..batched import CLUSTER_MAX, Batch
+
+        if ini_state is None and n <= CLUSTER_MAX[dt]:
+            # the 2 L n shifted circuits as one batched launch: each a whole
+            # forward run in shared memory, with its energy and (for shots)
+            # every term's <P_k>
+            b = Batch(device=dev, dtype=dt, grad=False, use_graph=False, term_expectations=need_terms)
+            for _ in range(rows):
+                b.add(self)
+            b.finalize()
+            b.params_flat[: rows * L * n].copy_(shifted.reshape(-1))
+            b.execute()
+            energies = b.expec[:rows]
             if need_terms and K:
-                nat.pauli_expectations_into(state, dt, dev, expec[r])
+                expec[:, :K] = b.term_expec_flat[: rows * K].reshape(rows, K)
+        else:
+            ini = nat.state_tensor(ini_state, dt, dev)
+            ws = nat.workspace(dt, _lib.QG_OP_RUN, dev)
+            energies = torch.empty(rows, dtype=torch.float64, device=dev)
+            state = torch.empty(2 ** n, dtype=_native.torch_dtype(dt), device=dev)
+            for r in range(rows):
+                nat.run_into(shifted[r], dt, dev, ini, ws, energies[r:r + 1], state if need_terms else None)
+                if need_terms and K:
+                    nat.pauli_expectations_into(state, dt, dev, expec[r])
         w = self._weights(dev)
         if component_sampling:
             k = torch.as_tensor(np.repeat(comps, 2), device=dev)

@@ -440,6 +440,8 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         const int np = J.kind == 0 ? L * n : 2 * L;
         for (int i = 0; i < np; ++i) J.grad[i] = 0.0;
       }
+      if (J.term_expec)
+        for (int k = 0; k < J.nterms; ++k) J.term_expec[k] = 0.0;
     }
     __syncthreads();
     for (int k = tid; k < J.nterms && k < BTERMS; k += NT) S.tw[k] = J.terms[k].w;
@@ -830,6 +832,49 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           *J.expec = (double)tot;
       }
       __syncthreads();
+    }
+    // ---- optional: <P_k> of every observable term on the final state (the
+    // per-term expectations the projector-shot estimators draw from,
+    // observable.py:82-177, base.py:22-46)
+    if (J.term_expec) {
+      for (int k = 0; k < J.nterms; ++k) {
+        const BatchTerm t = J.terms[k];
+        const uint32_t b0 = 1u << (n - 1 - t.q0);
+        R acc = (R)0;
+        for (int e = tid; e < M; e += NT) {
+          const uint32_t x = top | (uint32_t)e;
+          const C v = psi[swb(e, DBL)];
+          if (t.kind >= 2) {
+            bool sg = (x & b0) != 0;
+            if (t.kind == 3) sg ^= (x & (1u << (n - 1 - t.q1))) != 0;
+            const R p2 = fma(v.x, v.x, v.y * v.y);
+            acc += sg ? -p2 : p2;
+          } else {
+            const uint32_t xp = x ^ b0;
+            const C u = (xp >> m) != (x >> m) ? remote(psi)[swb((int)(xp & (uint32_t)(M - 1)), DBL)]
+                                              : psi[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
+            if (t.kind == 0) {
+              acc += fma(v.x, u.x, v.y * u.y);  // Re(conj(v) u)
+            } else {
+              // (Y psi)_x = -i psi_partner (bit 0) or +i psi_partner (bit 1)
+              const R sgn = (x & b0) ? (R)1 : (R)-1;
+              acc += sgn * fma(-v.x, u.y, v.y * u.x);  // Re(conj(v) i u) * sgn
+            }
+          }
+        }
+        const R v = wsum(acc);
+        if (lane == 0) S.red[warp][0] = v;
+        __syncthreads();
+        if (tid == 0) {
+          R tot = (R)0;
+          for (int w = 0; w < NT / 32; ++w) tot += S.red[w][0];
+          if (CS > 1)
+            atomicAdd(&J.term_expec[k], (double)tot);
+          else
+            J.term_expec[k] = (double)tot;
+        }
+        __syncthreads();
+      }
     }
     if (CS > 1) cluster.sync();
 

@@ -450,8 +450,7 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
     // occupancy per distinct shared-memory footprint (phase-table size, cost table)
     std::vector<std::pair<int64_t, std::pair<int, int>>> memo;
     for (const auto& d : P.sweeps) {
-      const int64_t key = ((int64_t)sweep_occupancy_class(d) << 40) | ((int64_t)d.nz << 32) |
-                          ((int64_t)(d.cost == COST_INT ? 1 : 0) << 31) | d.cost_maxabs;
+      const int64_t key = ((int64_t)d.nz << 32) | ((int64_t)(d.cost == COST_INT ? 1 : 0) << 31) | d.cost_maxabs;
       int pf = -1, pb = -1;
       for (const auto& mm : memo)
         if (mm.first == key) {

@@ -36,19 +36,6 @@ cudaError_t launch_cost_reduce(int n, const typename C2T<R>::T* lam, const typen
                                int cost, double w0, const int32_t* cost_i, const double* cost_d, double* partials,
                                int slot, int G, cudaStream_t st);
 
-// complex64 register-layout sweeps (qg_sweep_reg.cu): the 12-bit-tile sweeps
-// over high qubits run there (reg_sweep_applies).  The shared-memory round
-// trips a sweep needs in register layouts (0..2) set its shared memory and
-// so its occupancy class.
-bool reg_sweep_applies(const SweepDesc& d, bool bwd);
-size_t reg_sweep_smem(const SweepDesc& d, bool bwd);
-const void* reg_sweep_fn(const SweepDesc& d, bool bwd, bool uncompute);
-int sweep_occupancy_class(const SweepDesc& d);
-cudaError_t prepare_reg_sweep_kernels(int optin);
-cudaError_t launch_reg_sweep_fwd(const SweepDesc& d, const SweepPtrs<float>& p, int grid, cudaStream_t st, bool pdl);
-cudaError_t launch_reg_sweep_bwd(const SweepDesc& d, const SweepPtrs<float>& p, bool uncompute, int grid,
-                                 cudaStream_t st, bool pdl);
-
 cudaError_t launch_finalize(const double* partials, int G, int kind, int n, int nparam, int eslot, int neslots,
                             double* expec, double* grad, cudaStream_t st);
 

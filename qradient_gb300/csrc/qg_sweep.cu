@@ -1153,34 +1153,23 @@ cudaError_t prepare_sweep_kernels() {
     e = set_smem_limit(fn, optin);
     if (e != cudaSuccess) return e;
   }
-  e = prepare_reg_sweep_kernels(optin);
-  if (e != cudaSuccess) return e;
   ready[dev].store(1, std::memory_order_release);
   return cudaSuccess;
 }
 
-// The kernel a sweep launches.  complex64 sweeps over the high qubits of
-// 12-bit tiles (the default) run in the register-layout kernels
-// (qg_sweep_reg.cu, reg_sweep_applies); other sweeps over tiles of the
-// default size take the instantiation with the tile size fixed at compile
-// time; other tiles the runtime-size kernels.
+// The kernel a sweep launches: sweeps over tiles of the default size take
+// the instantiation with the tile size fixed at compile time.
 template <typename R>
 static bool fixed_tile(const SweepDesc& d) {
   return d.t == kTileFixed<R>;
 }
 template <typename R>
-static bool reg_sweep(const SweepDesc& d, bool bwd) {
-  return sizeof(R) == 4 && reg_sweep_applies(d, bwd);
-}
-template <typename R>
 static const void* fwd_pipe_fn(const SweepDesc& d) {
-  if (reg_sweep<R>(d, false)) return reg_sweep_fn(d, false, false);
   if (fixed_tile<R>(d)) return (const void*)sweep_fwd_pipe_kernel<R, kTileFixed<R>>;
   return (const void*)sweep_fwd_pipe_kernel<R, 0>;
 }
 template <typename R>
 static const void* bwd_fn(const SweepDesc& d, bool uncompute) {
-  if (reg_sweep<R>(d, true)) return reg_sweep_fn(d, true, uncompute);
   if (fixed_tile<R>(d))
     return uncompute ? (const void*)sweep_bwd_kernel<R, true, kTileFixed<R>>
                      : (const void*)sweep_bwd_kernel<R, false, kTileFixed<R>>;
@@ -1189,8 +1178,7 @@ static const void* bwd_fn(const SweepDesc& d, bool uncompute) {
 
 template <typename R>
 int sweep_ctas_per_sm(const SweepDesc& d, bool bwd, bool uncompute, bool pipe) {
-  const bool reg = reg_sweep<R>(d, bwd) && (bwd || pipe);
-  const size_t smem = reg ? reg_sweep_smem(d, bwd) : sweep_smem<R>(d, bwd, pipe && !bwd);
+  const size_t smem = sweep_smem<R>(d, bwd, pipe && !bwd);
   int blocks = 0;
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) {
@@ -1215,9 +1203,6 @@ cudaError_t launch_sweep_fwd(const SweepDesc& d, const SweepPtrs<R>& p, int grid
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
   if (pipe && d.start == START_LOAD) {
-    if constexpr (sizeof(R) == 4) {
-      if (reg_sweep<R>(d, false)) return launch_reg_sweep_fwd(d, p, grid, st, pdl);
-    }
     if (fixed_tile<R>(d))
       return launch_pdl(sweep_fwd_pipe_kernel<R, kTileFixed<R>>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
     return launch_pdl(sweep_fwd_pipe_kernel<R, 0>, grid, sweep_smem<R>(d, false, true), st, pdl, d, p);
@@ -1231,9 +1216,6 @@ cudaError_t launch_sweep_bwd(const SweepDesc& d, const SweepPtrs<R>& p, bool unc
   const size_t smem = sweep_smem<R>(d, true);
   cudaError_t e = prepare_sweep_kernels();
   if (e != cudaSuccess) return e;
-  if constexpr (sizeof(R) == 4) {
-    if (reg_sweep<R>(d, true)) return launch_reg_sweep_bwd(d, p, uncompute, grid, st, pdl);
-  }
   if (fixed_tile<R>(d)) {
     if (uncompute) return launch_pdl(sweep_bwd_kernel<R, true, kTileFixed<R>>, grid, smem, st, pdl, d, p);
     return launch_pdl(sweep_bwd_kernel<R, false, kTileFixed<R>>, grid, smem, st, pdl, d, p);

@@ -1,6 +1,5 @@
-// Device helpers shared by the sweep translation units (qg_sweep.cu, the
-// generic shared-memory sweeps; qg_sweep_reg.cu, the complex64
-// register-layout sweeps): launch with programmatic dependence, the CNOT
+// Device helpers of the sweep kernels (qg_sweep.cu): launch with
+// programmatic dependence, the CNOT
 // ladder as a GF(2)-linear index map, scaled-form rotations and their
 // gradient pair terms, the per-CTA setup (rotation forms, phase and cost
 // tables, tile bases) and the per-amplitude diagonal.

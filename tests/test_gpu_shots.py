@@ -173,3 +173,46 @@ def test_sample_expec_val_is_unbiased(golden):
     np.random.seed(5)
     v = circ.run_expec_val(exact_expec_val=False, shot_num=shots)
     assert abs(v - E) < 6 * sd
+
+
+def test_batched_term_expectations_and_shift_gradient():
+    """The batched kernel's per-term expectations (the projector estimators'
+    inputs) against qg_pauli_expectations on the same final states, for a
+    single-CTA complex128 job and a 2-CTA complex64 job with X, Y, Z and ZZ
+    terms; and the parameter-shift gradient through the batched launch
+    against the per-circuit path (forced by an explicit |0..0> start)."""
+    import torch
+
+    from qradient_gb300 import McClean
+    from qradient_gb300.batched import Batch
+
+    for n, L, dtype, tol in ((10, 3, "complex128", 1e-12), (14, 2, "complex64", 2e-5)):
+        rng = np.random.default_rng(n)
+        obs = {"zz": np.full((n, n), None), "x": np.full(n, None), "y": np.full(n, None), "z": np.full(n, None)}
+        obs["zz"][0, 1] = 0.7
+        obs["zz"][2, n - 1] = -0.4
+        obs["x"][0] = 0.3      # the top qubit: split across a 2-CTA job
+        obs["x"][n - 2] = 0.5
+        obs["y"][1] = -0.25
+        obs["z"][n // 2] = 0.9
+        c = McClean(n, obs, L, axes=rng.integers(0, 3, (L, n)), angles=rng.uniform(0, 2 * np.pi, (L, n)),
+                    dtype=dtype)
+        b = Batch(dtype=dtype, grad=False, use_graph=False, term_expectations=True)
+        P = [rng.uniform(0, 2 * np.pi, (L, n)) for _ in range(3)]
+        slots = [b.add(c, params=p) for p in P]
+        b.finalize()
+        b.execute()
+        torch.cuda.synchronize()
+        for slot, p in zip(slots, P):
+            c.angles = p
+            E = c.run_expec_val()
+            ref = c.pauli_expectations().cpu().numpy()
+            got = b.term_expec[slot].cpu().numpy()
+            assert abs(b.expec[slot].item() - E) <= tol * max(1.0, abs(E))
+            assert np.max(np.abs(got - ref)) <= tol, (n, got, ref)
+        c.angles = P[0]
+        E1, g1 = c.sample_grad(shot_num=None)
+        e0 = np.zeros(2 ** n, dtype=np.complex128)
+        e0[0] = 1.0
+        E2, g2 = c.sample_grad(shot_num=None, ini_state=e0)
+        assert abs(E1 - E2) <= tol and rel_err(g1, g2) <= tol, (n, rel_err(g1, g2))

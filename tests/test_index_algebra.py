@@ -152,76 +152,14 @@ def test_observable_diagonal_by_subset_sums_and_transform(n, t, seed):
             assert b[k] == pytest.approx(direct, abs=1e-12)
 
 
-# ---- complex64 register-layout sweeps (qg_sweep_reg.cu)
+# ---- batched kernel (qg_batched.cu, rotred_group)
 
-def _reg_layouts():
-    """local index of element k of thread (lane, warp) in layouts L1, L2, L3"""
-    return {
-        1: (lambda lane, warp: lane | (warp << 5), lambda k: k << 8),
-        3: (lambda lane, warp: (lane & 15) | ((lane >> 4) << 8) | (warp << 9), lambda k: k << 4),
-    }
-
-
-def test_register_layouts_cover_the_tile_once():
-    for lay, (thr, kp) in _reg_layouts().items():
-        seen = set()
-        for warp in range(8):
-            for lane in range(32):
-                t = thr(lane, warp)
-                for k in range(16):
-                    assert t & kp(k) == 0, (lay, lane, warp, k)  # disjoint parts
-                    seen.add(t | kp(k))
-        assert seen == set(range(4096)), lay
-
-
-def test_register_layout_transposes_are_free_of_bank_conflicts():
-    """Every 64-bit shared-memory access of a round trip (each layout, each
-    element k): the 16 lanes of a half warp reach 16 distinct 8-byte slots
-    modulo 128 bytes, and the swizzled address of thread part | element part
-    is the XOR of the parts' swizzled addresses."""
-    for lay, (thr, kp) in _reg_layouts().items():
-        for warp in range(8):
-            for k in range(16):
-                for half in (0, 16):
-                    slots = {sw64(thr(lane, warp) | kp(k)) % 16 for lane in range(half, half + 16)}
-                    assert len(slots) == 16, (lay, warp, k, half)
-                for lane in range(32):
-                    assert sw64(thr(lane, warp) | kp(k)) == sw64(thr(lane, warp)) ^ sw64(kp(k))
-
-
-def test_register_layout_global_offsets_and_coalescing():
-    """Element offsets: deposit(thread part | k part) = deposit(thread part)
-    + the sum of the element's in-thread bits' single-bit offsets; loads in
-    L1 and stores in L1 / L3 put 16 consecutive lanes on 16 consecutive
-    amplitudes (local bits 0..3 are the tile's lowest global bits)."""
-    rng = np.random.default_rng(3)
-    for _ in range(20):
-        n = int(rng.integers(13, 30))
-        low = list(range(4))
-        high = sorted(rng.choice(np.arange(4, n), 8, replace=False).tolist())
-        bits = low + high
-        for lay, (thr, kp) in _reg_layouts().items():
-            base = {1: 8, 3: 4}[lay]
-            o = [1 << bits[base + i] for i in range(4)]
-            for lane in range(32):
-                for warp in (0, 5):
-                    t = deposit(thr(lane, warp), bits)
-                    for k in range(16):
-                        off = sum(o[i] for i in range(4) if (k >> i) & 1)
-                        assert deposit(thr(lane, warp) | kp(k), bits) == t + off
-            for warp in range(8):
-                for k in range(16):
-                    for half in (0, 16):
-                        xs = [deposit(thr(lane, warp) | kp(k), bits) for lane in range(half, half + 16)]
-                        assert sorted(xs) == list(range(min(xs), min(xs) + 16)) and min(xs) % 16 == 0
-
-
-def test_register_sweep_rescaled_reductions():
-    """The backward register sweep takes a later phase's gradient sums after
-    the earlier phases' unscaled inverse rotations (R(-theta) / kappa) have
-    been applied to lambda and psi; the sums equal those at the end point
-    times 1/kappa^2 per such rotation.  Checked on a random 3-qubit state
-    pair with numpy matrices."""
+def test_rescaled_reductions_after_unscaled_inverse_rotations():
+    """The batched kernel's backward pass takes a rotation group's gradient
+    sums after the earlier groups' unscaled inverse rotations (R(-theta) /
+    kappa) have been applied to lambda and psi; the sums equal those at the
+    layer's end point times 1/kappa^2 per such rotation.  Checked on a
+    random 3-qubit state pair with numpy matrices."""
     rng = np.random.default_rng(9)
     X = np.array([[0, 1], [1, 0]], dtype=complex)
     Y = np.array([[0, -1j], [1j, 0]])
