@@ -17,6 +17,7 @@
 // the adjoint sweep (psi is rotated back instead of read from a history).
 #include <cooperative_groups.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "qg_batched.h"
 
@@ -1028,11 +1029,10 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
   }
 }
 
-template <typename R, int CS>
+template <typename R, int CS, int NT>
 static cudaError_t launch_one(const BatchJob* jobs, int njobs, int* counter, int mmax, cudaStream_t st,
                               int* grid_out) {
   using C = typename BatchC<R>::T;
-  constexpr int NT = BATCH_THREADS;
   const size_t smem = (size_t)(3 * (1 << mmax) + BATCH_TABLE) * sizeof(C);
   auto kern = batched_kernel<R, CS, NT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1067,11 +1067,19 @@ static cudaError_t launch_one(const BatchJob* jobs, int njobs, int* counter, int
 cudaError_t launch_batched(int dtype_double, int cluster, const BatchJob* jobs, int njobs, int* counter, int mmax,
                            cudaStream_t st, int* grid_out) {
   if (dtype_double) {
-    if (cluster == 2) return launch_one<double, 2>(jobs, njobs, counter, mmax, st, grid_out);
-    return launch_one<double, 1>(jobs, njobs, counter, mmax, st, grid_out);
+    if (cluster == 2) return launch_one<double, 2, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
+    return launch_one<double, 1, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
   }
-  if (cluster == 2) return launch_one<float, 2>(jobs, njobs, counter, mmax, st, grid_out);
-  return launch_one<float, 1>(jobs, njobs, counter, mmax, st, grid_out);
+  static const int wide = [] {
+    const char* v = getenv("QG_BATCH_THREADS_C64");
+    return v && atoi(v) == 1024;
+  }();
+  if (wide) {
+    if (cluster == 2) return launch_one<float, 2, 1024>(jobs, njobs, counter, mmax, st, grid_out);
+    return launch_one<float, 1, 1024>(jobs, njobs, counter, mmax, st, grid_out);
+  }
+  if (cluster == 2) return launch_one<float, 2, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
+  return launch_one<float, 1, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
 }
 
 }  // namespace qg
