@@ -17,7 +17,6 @@
 // the adjoint sweep (psi is rotated back instead of read from a history).
 #include <cooperative_groups.h>
 #include <stdint.h>
-#include <stdlib.h>
 
 #include "qg_batched.h"
 
@@ -1069,14 +1068,6 @@ cudaError_t launch_batched(int dtype_double, int cluster, const BatchJob* jobs, 
   if (dtype_double) {
     if (cluster == 2) return launch_one<double, 2, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
     return launch_one<double, 1, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
-  }
-  static const int wide = [] {
-    const char* v = getenv("QG_BATCH_THREADS_C64");
-    return v && atoi(v) == 1024;
-  }();
-  if (wide) {
-    if (cluster == 2) return launch_one<float, 2, 1024>(jobs, njobs, counter, mmax, st, grid_out);
-    return launch_one<float, 1, 1024>(jobs, njobs, counter, mmax, st, grid_out);
   }
   if (cluster == 2) return launch_one<float, 2, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
   return launch_one<float, 1, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);

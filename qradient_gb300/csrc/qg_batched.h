@@ -11,6 +11,9 @@ namespace qg {
 using BatchJob = qg_batch_job;
 using BatchTerm = qg_term;
 
+// threads per CTA: 512 (16 warps).  Measured with 1024 (complex64: 64
+// registers a thread, 240 bytes spilled) the n = 14 jobs ran at 60.4k against
+// 82.9k circuits/s, the n = 12 ones at 279k against 397k.
 constexpr int BATCH_THREADS = 512;
 constexpr int BATCH_TABLE = 1024;   // phase-table entries (Z rotations or the QAOA cost)
 
