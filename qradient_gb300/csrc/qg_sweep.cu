@@ -249,95 +249,6 @@ __device__ __forceinline__ void apply_all4(C* v, int tsize, const SweepDesc& d, 
   }
 }
 
-// Tile bits of a sweep as two contiguous runs of global bits, [0, nlow) and
-// [hb, hb + t - nlow) (every tile the layout builds: sweep A is one run, the
-// high-bit sweeps keep the lowest bits): then the global offset of a local
-// index l is (l & (2^nlow - 1)) | ((l >> nlow) << hb), three integer
-// operations instead of a loop over the bits.
-struct TwoRuns {
-  int nlow, hb;
-  bool ok;
-};
-__device__ __forceinline__ TwoRuns two_runs(const SweepDesc& d, int t) {
-  TwoRuns r{0, 0, true};
-  while (r.nlow < t && d.bits[r.nlow] == r.nlow) ++r.nlow;
-  r.hb = r.nlow < t ? d.bits[r.nlow] : 0;
-  for (int i = r.nlow; i < t; ++i) r.ok &= d.bits[i] == r.hb + (i - r.nlow);
-  return r;
-}
-__device__ __forceinline__ uint64_t dep_runs(int l, const TwoRuns& r) {
-  return (uint64_t)(l & ((1 << r.nlow) - 1)) | ((uint64_t)(l >> r.nlow) << r.hb);
-}
-
-// complex64 forward sweeps over 12-bit tiles: the top group of four
-// rotations reads its tasks from shared memory, rotates them and writes
-// them straight to global memory with the commuting diagonal, so the
-// separate store pass (one more shared-memory read of every amplitude)
-// goes.  The caller checks, uniformly per sweep, that the group's bits are
-// all >= 4 -- each task is one thread's (4096 >> 4 = 256 tasks), and the
-// lanes of a warp then run along local bits 0..3: 16 consecutive amplitudes
-// per half warp -- and that the tile is two runs (dep_runs).  zlo[j] is the
-// Z-table pattern of local index j < 256, S.zpk[k] that of k << 8.
-template <typename C, typename R>
-__device__ __forceinline__ void store_group4(const C* v, const SweepDesc& d, const SetupShared& S, int g0,
-                                             const TwoRuns& runs, int64_t tile_base, bool diag, const int* zlo,
-                                             const C* ztab, const C* ctab, const SweepPtrs<R>& p, double gamma,
-                                             bool fold) {
-  int b[4], ax[4], fm[4];
-  R uu[4];
-  uint64_t go[4];
-  int zg[4], sbit[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    b[i] = d.xy[g0 + i].lbit;
-    ax[i] = d.xy[g0 + i].axis;
-    fm[i] = S.form[g0 + i];
-    uu[i] = (R)S.uf[g0 + i];
-    go[i] = dep_runs(1 << b[i], runs);
-    zg[i] = zlo[(1 << b[i]) & 255] | S.zpk[(1 << b[i]) >> 8];
-    sbit[i] = sw<R>(1 << b[i]);
-  }
-  int base = threadIdx.x;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) base = insert0(base, b[i]);
-  const int sb = sw<R>(base);
-  C el[16];
-#pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    int x = sb;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if ((c >> i) & 1) x ^= sbit[i];
-    el[c] = v[x];
-  }
-  rot_block_any<1, 0, 4>(el, ax[0], fm[0], uu[0]);
-  rot_block_any<1, 1, 4>(el, ax[1], fm[1], uu[1]);
-  rot_block_any<1, 2, 4>(el, ax[2], fm[2], uu[2]);
-  rot_block_any<1, 3, 4>(el, ax[3], fm[3], uu[3]);
-  const uint64_t xb = (uint64_t)tile_base | dep_runs(base, runs);
-  C* out = p.psi_out + xb;
-  const int zb = zpattern((uint64_t)tile_base, d) | zlo[base & 255] | S.zpk[base >> 8];
-#pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    uint64_t off = 0;
-    int zp = zb;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if ((c >> i) & 1) {
-        off += go[i];
-        zp |= zg[i];
-      }
-    C e = el[c];
-    if (diag) {
-      if (d.cost == COST_NONE && d.nz > 0)
-        e = cmul(e, ztab[zp]);
-      else
-        e = apply_diag<C>(e, xb + off, zp, d, ztab, ctab, p.cost_i, p.cost_d, gamma, fold, false);
-    }
-    out[off] = e;
-  }
-}
-
 template <typename C, typename R, int SG>
 __device__ __forceinline__ void apply_all(C* v, C* v2, int tsize, const SweepDesc& d, const SetupShared& S) {
   for (int g0 = 0; g0 < d.nxy; g0 += 3) {
@@ -481,18 +392,6 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
   // pointer plus offhi[k] (the parts are disjoint).
   TileBases tb(S.outside, n - t, n, d.bits, t);
   const int stid = sw<R>(tid);
-  // complex64, 12-bit tiles: the top group of four rotations stores straight
-  // to global memory where its bits allow (store_group4)
-  constexpr bool kDirect = sizeof(R) == 4 && TB == 12;
-  __shared__ int zlo[kDirect ? 256 : 1];
-  bool direct = false;
-  TwoRuns runs{0, 0, false};
-  if constexpr (kDirect) {
-    zlo[tid] = zpt;
-    runs = two_runs(d, t);
-    direct = runs.ok && runs.nlow >= 4 && d.nxy >= 4 && d.xy[d.nxy - 4].lbit >= 4;
-    __syncthreads();
-  }
 
   // copies of one tile into dst: this thread's elements only
   const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts'
@@ -548,29 +447,6 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
       }
     }
     __syncthreads();
-    if constexpr (kDirect) {
-      if (direct) {
-        // the groups below the top four (the remainder first), then the top
-        // group straight to global memory
-        const int rem = d.nxy & 3;
-        if (rem == 3)
-          apply_group<C, R, 3, 1>(tile, nullptr, tsize, d, S, 0);
-        else if (rem == 2)
-          apply_group<C, R, 2, 1>(tile, nullptr, tsize, d, S, 0);
-        else if (rem == 1)
-          apply_group<C, R, 1, 1>(tile, nullptr, tsize, d, S, 0);
-        if (rem) __syncthreads();
-        for (int g0 = rem; g0 + 4 < d.nxy; g0 += 4) {
-          apply_group<C, R, 4, 1>(tile, nullptr, tsize, d, S, g0);
-          __syncthreads();
-        }
-        store_group4<C, R>(tile, d, S, d.nxy - 4, runs, base, diag_store, zlo, ztab, ctab, p, gamma, fold);
-        __syncthreads();  // the buffer is refilled by the copies issued next iteration
-        cur ^= 1;
-        bcur = bnext;
-        continue;
-      }
-    }
     if constexpr (sizeof(R) == 4)
       apply_all4<C, R>(tile, tsize, d, S);
     else

@@ -181,48 +181,3 @@ def test_rescaled_reductions_after_unscaled_inverse_rotations():
     ref = np.imag(np.vdot(lam, on(Y, 1) @ psi))
     got = np.imag(np.vdot(M @ lam, on(Y, 1) @ (M @ psi)))
     assert abs(got * kappa ** 2 - ref) < 1e-12
-
-
-# ---- direct stores of the top rotation group (complex64 forward sweeps)
-
-def _tiles(n, t=12, c=4):
-    tiles = [list(range(t))]
-    nxt = t
-    while nxt < n:
-        k = min(t - c, n - nxt)
-        tiles.append(list(range(t - k)) + list(range(nxt, nxt + k)))
-        nxt += k
-    return tiles
-
-
-def test_two_run_deposit_and_direct_store_coalescing():
-    """Every tile the layout builds is two runs of global bits, [0, nlow)
-    and [hb, ...), so deposit(l) = (l & (2^nlow - 1)) | ((l >> nlow) << hb);
-    and a group of four rotation bits all >= 4 leaves one task per thread
-    whose base runs, across 16 lanes, over 16 consecutive amplitudes."""
-
-    def insert0(p, j):
-        return ((p >> j) << (j + 1)) | (p & ((1 << j) - 1))
-
-    rng = np.random.default_rng(5)
-    for n in (12, 13, 18, 20, 24, 28, 30):
-        for bits in _tiles(n):
-            nlow = 0
-            while nlow < len(bits) and bits[nlow] == nlow:
-                nlow += 1
-            hb = bits[nlow] if nlow < len(bits) else 0
-            assert all(bits[i] == hb + i - nlow for i in range(nlow, len(bits)))
-            assert nlow >= 4
-            for l in range(0, 4096, 7):
-                assert deposit(l, bits) == (l & ((1 << nlow) - 1)) | ((l >> nlow) << hb)
-            for _ in range(5):
-                g = sorted(rng.choice(np.arange(4, 12), 4, replace=False).tolist())
-                for warp in range(8):
-                    for half in (0, 16):
-                        xs = []
-                        for lane in range(half, half + 16):
-                            base = warp * 32 + lane
-                            for j in g:
-                                base = insert0(base, j)
-                            xs.append(deposit(base, bits))
-                        assert xs == list(range(xs[0], xs[0] + 16)) and xs[0] % 16 == 0
