@@ -205,3 +205,65 @@ def test_batched_autograd_n14_complex64_vs_fd():
             assert abs(gk[i, q] - g0[i, q]) <= 1e-4 * max(1.0, np.max(np.abs(g0)))
     print("batched complex64 n=14 L=30: normwise gradient error vs FP64 oracle %.2e" % worst)
     assert worst <= 1e-4
+
+
+def test_config3_full_batch_and_complex128_check():
+    """Config 3 as stated: 4096 parameter vectors (uniform [0, 2 pi)) of a
+    McClean n=14 L=30 circuit with shared random axes in one CUDA-graph
+    replay, complex64 with FP32 sums, every job's E and gradient written;
+    sampled jobs against the FP64 oracle (the reference's grad_run
+    restated, mc_clean.py:47-78) and against central differences (h =
+    1e-5) of complex128 runs; and the complex128 check: n=14 complex128 jobs
+    exceed the 2-CTA limit (13), so they run on the sweep path inside the
+    same graph, checked against the oracle to 1e-12."""
+    import torch
+
+    from qradient_gb300 import McClean
+    from qradient_gb300.batched import mcclean_batch
+
+    n, L, B = 14, 30, 4096
+    rng = np.random.default_rng(3)
+    axes = rng.integers(0, 3, (L, n))
+    zz = np.full((n, n), None)
+    for i in range(n - 1):
+        zz[i, i + 1] = 1.0
+    t = O.Terms(np.full(n - 1, 3), np.arange(n - 1), np.arange(1, n), np.ones(n - 1))
+    P = rng.uniform(0, 2 * np.pi, (B, L * n))
+    b = mcclean_batch(n, L, axes, {"zz": zz}, B, dtype="complex64")
+    b.params_flat.copy_(torch.as_tensor(P.reshape(-1), device=b.params_flat.device))
+    E, _ = b.grad()
+    E, _ = b.grad()  # the graph replay
+    torch.cuda.synchronize()
+    Eh = E.cpu().numpy()
+    G = b.grads_flat.cpu().numpy().reshape(B, L, n)
+    assert np.all(np.isfinite(Eh)) and np.all(np.isfinite(G))
+    ref = McClean(n, {"zz": zz}, L, axes=axes, angles=np.zeros((L, n)), dtype="complex128")
+    worst = 0.0
+    for k in rng.choice(B, 6, replace=False):
+        E0, g0 = O.mcclean_grad(n, axes, P[k].reshape(L, n), t)
+        worst = max(worst, rel_err(G[k], g0))
+        assert abs(Eh[k] - E0) <= 1e-4, k
+        for (i, q) in ((0, 0), (L - 1, n - 1)):
+            h = 1e-5
+            a = P[k].reshape(L, n).copy()
+            a[i, q] += h
+            ref.angles = a
+            ep = ref.run_expec_val()
+            a[i, q] -= 2 * h
+            ref.angles = a
+            em = ref.run_expec_val()
+            assert abs((ep - em) / (2 * h) - g0[i, q]) < 1e-8
+            assert abs(G[k, i, q] - g0[i, q]) <= 1e-4 * max(1.0, np.max(np.abs(g0)))
+    print("config 3, 4096 vectors, complex64: worst normwise gradient error of 6 sampled jobs vs FP64 %.2e" % worst)
+    assert worst <= 1e-4
+    # the complex128 check (the sweep path inside the graph)
+    B2 = 32
+    b2 = mcclean_batch(n, L, axes, {"zz": zz}, B2, dtype="complex128")
+    b2.params_flat.copy_(torch.as_tensor(P[:B2].reshape(-1), device=b2.params_flat.device))
+    b2.grad()
+    E2, _ = b2.grad()
+    torch.cuda.synchronize()
+    G2 = b2.grads_flat.cpu().numpy().reshape(B2, L, n)
+    for k in (0, B2 - 1):
+        E0, g0 = O.mcclean_grad(n, axes, P[k].reshape(L, n), t)
+        assert abs(E2[k].item() - E0) <= 1e-12 and rel_err(G2[k], g0) <= 1e-12, (k, rel_err(G2[k], g0))
