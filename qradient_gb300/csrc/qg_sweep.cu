@@ -86,17 +86,24 @@ __device__ __forceinline__ void apply_group(C* v, C* v2, int tsize, const SweepD
   }
 }
 
+// Per-thread sums across tiles (ACC): a thread's pair sums of rotation g
+// continue in accs[g * NTHREADS + tid] from tile to tile -- loaded into the
+// FMA chain and stored back, so no add is spent per tile -- and are summed
+// over the CTA's threads once, at its end.  Without ACC each group's sums
+// go through a warp reduction per tile (red_add3), whose adds (0.76 per
+// amplitude per group of three in complex128) take FP64 pipe slots.
+
 // gradient reductions of a group of G rotations (read-only)
-template <typename C, typename R, int G>
+template <typename C, typename R, int G, bool ACC = false>
 __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize, const SweepDesc& d,
-                                             SetupShared& S, int g0) {
+                                             SetupShared& S, int g0, R* accs = nullptr) {
   int b[G], ax[G];
   R acc[G];
 #pragma unroll
   for (int i = 0; i < G; ++i) {
     b[i] = d.xy[g0 + i].lbit;
     ax[i] = d.xy[g0 + i].axis;
-    acc[i] = (R)0;
+    acc[i] = ACC ? accs[(g0 + i) * NTHREADS + threadIdx.x] : (R)0;
   }
   int sbit[sizeof(R) == 4 ? G : 1];
   if constexpr (sizeof(R) == 4) {
@@ -145,7 +152,12 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
       }
     }
   }
-  red_add3<R, G>(S, RS_XY + g0, acc);
+  if constexpr (ACC) {
+#pragma unroll
+    for (int i = 0; i < G; ++i) accs[(g0 + i) * NTHREADS + threadIdx.x] = acc[i];
+  } else {
+    red_add3<R, G>(S, RS_XY + g0, acc);
+  }
 }
 
 // The last gate group of a backward sweep: its gradient reductions and its
@@ -153,8 +165,9 @@ __device__ __forceinline__ void reduce_group(const C* tl, const C* tp, int tsize
 // reduces, rotates lambda -- and psi when PSI -- and writes them back).  The
 // reductions of the sweep's other groups must have been taken before: every
 // reduction sees lambda and psi before any inverse rotation.
-template <typename C, typename R, int G, bool PSI>
-__device__ __forceinline__ void redrot_group(C* tl, C* tp, int tsize, const SweepDesc& d, SetupShared& S, int g0) {
+template <typename C, typename R, int G, bool PSI, bool ACC = false>
+__device__ __forceinline__ void redrot_group(C* tl, C* tp, int tsize, const SweepDesc& d, SetupShared& S, int g0,
+                                             R* accs = nullptr) {
   int b[G], ax[G], fm[G];
   R uu[G], acc[G];
 #pragma unroll
@@ -163,7 +176,7 @@ __device__ __forceinline__ void redrot_group(C* tl, C* tp, int tsize, const Swee
     ax[i] = d.xy[g0 + i].axis;
     fm[i] = S.form[g0 + i];
     uu[i] = sizeof(R) == 4 ? (R)S.uf[g0 + i] : (R)S.u[g0 + i];
-    acc[i] = (R)0;
+    acc[i] = ACC ? accs[(g0 + i) * NTHREADS + threadIdx.x] : (R)0;
   }
   int sbit[sizeof(R) == 4 ? G : 1];
   if constexpr (sizeof(R) == 4) {
@@ -228,7 +241,12 @@ __device__ __forceinline__ void redrot_group(C* tl, C* tp, int tsize, const Swee
       for (int c = 0; c < (1 << G); ++c) tp[idx[c]] = qa[c];
     }
   }
-  red_add3<R, G>(S, RS_XY + g0, acc);
+  if constexpr (ACC) {
+#pragma unroll
+    for (int i = 0; i < G; ++i) accs[(g0 + i) * NTHREADS + threadIdx.x] = acc[i];
+  } else {
+    red_add3<R, G>(S, RS_XY + g0, acc);
+  }
 }
 
 // complex64 forward sweeps: groups of four rotations (16 amplitudes per
@@ -502,6 +520,14 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   C* tp = tl + tsize;
   C* ztab = tp + tsize;
   C* ctab = ztab + (1 << d.nz);
+  // complex128: per-thread gradient sums kept across tiles in shared memory
+  // (reduce_group, ACC); complex64 keeps the per-tile warp reductions (three
+  // resident CTAs leave no room for the 13 x 256 sums)
+  constexpr bool kAcc = sizeof(R) == 8;
+  R* accs = kAcc ? (R*)(ctab + (d.cost == COST_INT ? 2 * d.cost_maxabs + 1 : 0)) : nullptr;
+  if constexpr (kAcc) {
+    for (int g = 0; g < TMAX; ++g) accs[g * NTHREADS + threadIdx.x] = (R)0;
+  }
   __shared__ int64_t ladk[sizeof(R) == 4 ? 32 : 1];  // complex64 only
   sweep_setup<C, true>(d, p.params, S, ztab, ctab, sizeof(R) == 4 ? ladk : nullptr);
   pdl_trigger();
@@ -677,26 +703,26 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
       for (int g0 = 0; g0 < d.nxy; g0 += 3) {
         const int g = d.nxy - g0 < 3 ? d.nxy - g0 : 3;
         if (g == 3)
-          reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+          reduce_group<C, R, 3, kAcc>(tl, tp, tsize, d, S, g0, accs);
         else if (g == 2)
-          reduce_group<C, R, 2>(tl, tp, tsize, d, S, g0);
+          reduce_group<C, R, 2, kAcc>(tl, tp, tsize, d, S, g0, accs);
         else
-          reduce_group<C, R, 1>(tl, tp, tsize, d, S, g0);
+          reduce_group<C, R, 1, kAcc>(tl, tp, tsize, d, S, g0, accs);
       }
       __syncthreads();
     }
     const int glast = !kFuse ? d.nxy : d.nxy > 0 ? ((d.nxy - 1) / 3) * 3 : 0;
     if (kFuse)
-      for (int g0 = 0; g0 < glast; g0 += 3) reduce_group<C, R, 3>(tl, tp, tsize, d, S, g0);
+      for (int g0 = 0; g0 < glast; g0 += 3) reduce_group<C, R, 3, kAcc>(tl, tp, tsize, d, S, g0, accs);
     if (kFuse && d.nxy > 0) {
       if (glast > 0) __syncthreads();  // the fused pass rewrites what the reductions above read
       const int g = d.nxy - glast;
       if (g == 3)
-        redrot_group<C, R, 3, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
+        redrot_group<C, R, 3, UNCOMPUTE, kAcc>(tl, tp, tsize, d, S, glast, accs);
       else if (g == 2)
-        redrot_group<C, R, 2, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
+        redrot_group<C, R, 2, UNCOMPUTE, kAcc>(tl, tp, tsize, d, S, glast, accs);
       else
-        redrot_group<C, R, 1, UNCOMPUTE>(tl, tp, tsize, d, S, glast);
+        redrot_group<C, R, 1, UNCOMPUTE, kAcc>(tl, tp, tsize, d, S, glast, accs);
       __syncthreads();
     }
     // history mode: psi is not read again in this tile (every pass above
@@ -750,6 +776,13 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
   }
   cp_async_wait<0>();
 
+  // X/Y rotations (kAcc): each thread's sums across its tiles into the warp slots
+  if constexpr (kAcc) {
+    for (int g = 0; g < d.nxy; ++g) {
+      const R v = warp_sum(accs[g * NTHREADS + tid]);
+      if ((tid & 31) == 0) red_slot_add<R>(S, tid >> 5, RS_XY + g, v);
+    }
+  }
   // Z rotations: per-thread sums into the warp slots once per CTA
   if (d.nz > 0) {
     for (int j = 0; j < d.nz; ++j) {
@@ -1106,6 +1139,8 @@ static size_t sweep_smem(const SweepDesc& d, bool bwd, bool pipe = false) {
   size_t s = (size_t)(bwd || pipe ? 2 : 1) * ((size_t)1 << d.t) * sizeof(C);
   s += ((size_t)1 << d.nz) * sizeof(C);
   if (d.cost == COST_INT) s += (size_t)(2 * d.cost_maxabs + 1) * sizeof(C);
+  // complex128 backward: the per-thread gradient sums (sweep_bwd_kernel, kAcc)
+  if (bwd && sizeof(R) == 8) s += (size_t)TMAX * NTHREADS * sizeof(R);
   return s;
 }
 
