@@ -410,6 +410,9 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
   // pointer plus offhi[k] (the parts are disjoint).
   TileBases tb(S.outside, n - t, n, d.bits, t);
   const int stid = sw<R>(tid);
+  // complex64 fixed tiles: element-loop parts from registers (KParts)
+  constexpr bool kRegK = TB > 8 && sizeof(R) == 4;
+  constexpr int KB = TB > 8 ? TB - 8 : 1, NK = 1 << KB;
 
   // copies of one tile into dst: this thread's elements only
   const uint64_t ldep = ladder_inv((uint64_t)dep_lo, lm);  // ladder images are linear: XOR of the parts'
@@ -421,7 +424,20 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
       // images; complex128, bound by the FP64 pipe, has one loop that
       // computes the image (measured: a shared-memory load cost more there
       // than the integer work)
-      if constexpr (sizeof(R) == 4) {
+      if constexpr (kRegK) {
+        if (d.pre == ENT_CNOT) {
+          const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
+          const KParts<int64_t, KB> L(ladk);
+#pragma unroll
+          for (int k = 0; k < NK; ++k)
+            cp_async_elem(&dst[stid + k * NTHREADS], p.psi_in + (lbase ^ (uint64_t)L.at(k)));
+        } else {
+          const C* pin = p.psi_in + bd;
+          const KParts<int64_t, KB> H(S.offhi);
+#pragma unroll
+          for (int k = 0; k < NK; ++k) cp_async_elem(&dst[stid + k * NTHREADS], pin + H.sum(k));
+        }
+      } else if constexpr (sizeof(R) == 4) {
         if (d.pre == ENT_CNOT) {
           const uint64_t lbase = ladder_inv((uint64_t)base, lm) ^ ldep;
           for (int k = 0; k < nk; ++k) cp_async_elem(&dst[stid + k * NTHREADS], p.psi_in + (lbase ^ (uint64_t)ladk[k]));
@@ -472,7 +488,19 @@ __global__ void __launch_bounds__(NTHREADS, 3) sweep_fwd_pipe_kernel(const __gri
     if (sizeof(R) == 4 && active && diag_store && d.cost == COST_NONE && d.nz > 0) {
       // complex64, the merged Z table alone: no per-element case tests
       C* out = p.psi_out + bd;
-      for (int k = 0; k < nk; ++k) out[S.offhi[k]] = cmul(tile[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
+      if constexpr (kRegK) {
+        const KParts<int64_t, KB> H(S.offhi);
+        const KParts<int, KB> Z(S.zpk);
+#pragma unroll
+        for (int k = 0; k < NK; ++k) out[H.sum(k)] = cmul(tile[stid + k * NTHREADS], ztab[zp | Z.at(k)]);
+      } else {
+        for (int k = 0; k < nk; ++k) out[S.offhi[k]] = cmul(tile[stid + k * NTHREADS], ztab[zp | S.zpk[k]]);
+      }
+    } else if (kRegK && active && !diag_store) {
+      C* out = p.psi_out + bd;
+      const KParts<int64_t, KB> H(S.offhi);
+#pragma unroll
+      for (int k = 0; k < NK; ++k) out[H.sum(k)] = tile[stid + k * NTHREADS];
     } else if (active) {
       C* out = p.psi_out + bd;
       if (sizeof(R) == 8 || diag_store) {
@@ -594,6 +622,23 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     } else {
       cp_async_elem(&tp[stid + k * NTHREADS], p.psi_in + bd_ + oh);
     }
+  };
+  // complex64 fixed tiles: the same copies with the element-loop parts from
+  // registers (KParts; the loops calling these unroll over k)
+  constexpr bool kRegK = TB > 8 && sizeof(R) == 4;
+  constexpr int KB = TB > 8 ? TB - 8 : 1, NK = 1 << KB;
+  using KP64 = KParts<int64_t, KB>;
+  auto lam_copy_r = [&](int k, uint64_t bd_, uint64_t lbase_, const KP64& H, const KP64& L) {
+    if (d.lam_undo == ENT_CNOT)
+      cp_async_elem(&tl[stid + k * NTHREADS], p.lam_in + (lbase_ ^ (uint64_t)L.at(k)));
+    else
+      cp_async_elem(&tl[stid + k * NTHREADS], p.lam_in + bd_ + H.sum(k));
+  };
+  auto psi_copy_r = [&](int k, uint64_t bd_, uint64_t lbase_, const KP64& H, const KP64& L) {
+    if (d.psi_undo == ENT_CNOT)
+      cp_async_elem(&tp[stid + k * NTHREADS], p.psi_in + (lbase_ ^ (uint64_t)L.at(k)));
+    else
+      cp_async_elem(&tp[stid + k * NTHREADS], p.psi_in + bd_ + H.sum(k));
   };
   // The next tile's copies go out early, so that their DRAM round trip
   // overlaps the rest of this tile's work: each element's as soon as this
@@ -728,7 +773,13 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     // history mode: psi is not read again in this tile (every pass above
     // that reads it ended at a barrier): the next tile's psi copies go out now
     if (!UNCOMPUTE && active && more) {
-      for (int k = 0; k < nk; ++k) psi_copy(k, bdn, lbasen);
+      if constexpr (kRegK) {
+        const KP64 H(S.offhi), L(ladk);
+#pragma unroll
+        for (int k = 0; k < NK; ++k) psi_copy_r(k, bdn, lbasen, H, L);
+      } else {
+        for (int k = 0; k < nk; ++k) psi_copy(k, bdn, lbasen);
+      }
     }
     if (kFuse) {
       for (int g0 = 0; g0 < glast; g0 += 3) {
@@ -741,7 +792,25 @@ __global__ void __launch_bounds__(NTHREADS, sizeof(R) == 4 ? 3 : 2) sweep_bwd_ke
     // (each stored element's slots take the next tile's copies at once: only
     // this thread reads its slots here)
     const bool pf = more;
-    if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
+    if (kRegK && active && !UNCOMPUTE && d.cost == COST_NONE && (!d.has_diag || d.nz > 0)) {
+      // the two cases below with the element-loop parts from registers
+      C* lout = p.lam_out + bd;
+      const KP64 H(S.offhi), L(ladk);
+      if (!d.has_diag) {
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+          lout[H.sum(k)] = tl[stid + k * NTHREADS];
+          if (pf) lam_copy_r(k, bdn, lbasen, H, L);
+        }
+      } else {
+        const KParts<int, KB> Z(S.zpk);
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+          lout[H.sum(k)] = cmul(tl[stid + k * NTHREADS], ztab[zp | Z.at(k)]);
+          if (pf) lam_copy_r(k, bdn, lbasen, H, L);
+        }
+      }
+    } else if (sizeof(R) == 4 && active && !UNCOMPUTE && !d.has_diag && d.cost == COST_NONE) {
       // nothing diagonal to apply and no psi to write: a plain copy-out
       C* lout = p.lam_out + bd;
       for (int k = 0; k < nk; ++k) {

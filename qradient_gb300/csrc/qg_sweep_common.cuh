@@ -283,6 +283,37 @@ __device__ __forceinline__ int64_t deposit(int64_t v, const uint8_t* bits, int n
   return x;
 }
 
+// Element-loop parts in registers (fixed tiles).  With a tile of TB bits the
+// element-loop index k has KB = TB - 8 bits, and offhi[k], zpk[k] and ladk[k]
+// are GF(2)-linear in k (deposit, the Z-table pattern and the ladder image
+// are): each is the XOR of its values at k's single bits, and for offhi,
+// whose parts are disjoint, also their sum.  A loop unrolled over k builds
+// them from KB registers loaded before the loop instead of one
+// shared-memory load per element.
+template <typename T, int KB>
+struct KParts {
+  T v[KB];
+  __device__ __forceinline__ explicit KParts(const T* tab) {
+#pragma unroll
+    for (int i = 0; i < KB; ++i) v[i] = tab[1 << i];
+  }
+  // k is a compile-time constant in an unrolled loop
+  __device__ __forceinline__ T at(int k) const {
+    T x = 0;
+#pragma unroll
+    for (int i = 0; i < KB; ++i)
+      if ((k >> i) & 1) x ^= v[i];
+    return x;
+  }
+  __device__ __forceinline__ T sum(int k) const {
+    T x = 0;
+#pragma unroll
+    for (int i = 0; i < KB; ++i)
+      if ((k >> i) & 1) x += v[i];
+    return x;
+  }
+};
+
 // The bases of a CTA's tiles (tile ids blockIdx.x, + gridDim.x, ...) in
 // turn: deposit(v + g) is deposit(v) plus deposit(g) with the carries passed
 // through the tile's own bits, a masked add of three operations per tile
