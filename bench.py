@@ -742,8 +742,9 @@ def main():
                                    "profiles/backward_sweep_traffic.json) / their mean duration (CUDA events "
                                    "around every launch on the launching stream)",
                 "fp64_pipe_busy_ncu": prof.get("pipe_busy"),
-                # the survey's credited count (6 flops per rotation, 4 per
-                # reduction, per amplitude) at the same duration, for reference
+                # the credited algorithmic count (6 flops per rotation as the
+                # reference's gate formula writes it, 4 per reduction, per
+                # amplitude) at the same duration, for reference
                 "algorithmic_rate_tflops": (2 ** args.n) * args.n * (4 + 6) * args.layers / bwd_per_step /
                                            bwd_avg_s * 1e-12 if bwd_n else None,
                 "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",

@@ -182,6 +182,21 @@ __device__ __forceinline__ void rot_pair_t(C& a, C& b, R u) {
       b.x = fma(u, b0.x, SG > 0 ? a0.y : -a0.y);
       b.y = fma(u, b0.y, SG > 0 ? -a0.x : a0.x);
     }
+  } else if constexpr (sizeof(R) == 4) {
+    // complex64 Y forms act componentwise on (x, y): one paired FP32 FMA
+    // (FFMA2) per amplitude instead of two
+    const float2 a2 = *reinterpret_cast<const float2*>(&a0), b2 = *reinterpret_cast<const float2*>(&b0);
+    float2 ra, rb;
+    if (FORM == 0) {
+      ra = __ffma2_rn(make_float2(-us, -us), b2, a2);
+      rb = __ffma2_rn(make_float2(us, us), a2, b2);
+    } else {
+      const float2 uu = make_float2(u, u);
+      ra = __ffma2_rn(uu, a2, SG > 0 ? make_float2(-b2.x, -b2.y) : b2);
+      rb = __ffma2_rn(uu, b2, SG > 0 ? a2 : make_float2(-a2.x, -a2.y));
+    }
+    a = *reinterpret_cast<const C*>(&ra);
+    b = *reinterpret_cast<const C*>(&rb);
   } else {
     if (FORM == 0) {
       a.x = fma(-us, b0.x, a0.x);
