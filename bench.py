@@ -24,6 +24,8 @@ The default run adds, measured in the same process after the headline:
   c64        the same circuit in complex64 (HBM-bound), with its HBM fraction
   cz_after   the same circuit with the CZ ladder after the rotations
   qaoa       QAOA MaxCut n=24 p=10 complex128
+  large      McClean n=28 L=50 complex128 (its state history does not fit in
+             HBM: the uncompute form of the adjoint sweep)
   batched    4096 parameter vectors of McClean n=14 L=30 complex64 in one
              CUDA-graph replay, against the plain per-call path
   served     Poisson streams through the continuous-batching server (the
@@ -284,19 +286,20 @@ def _events(dev):
             torch.cuda.current_stream(dev))
 
 
-def measure_mcclean(n, L, seed, dtype, entangler, placement, steps, warmup, dev):
+def measure_mcclean(n, L, seed, dtype, entangler, placement, steps, warmup, dev, min_warmup=3):
     """grad_run circuits/s of one McClean chain circuit (device-resident
     angles), with its step-level HBM fraction of the compulsory bytes."""
     import torch
 
     from qradient_gb300 import McClean
+    from qradient_gb300 import _lib, _native
 
     axes, angles, obs = workload(n, L, seed)
     c = McClean(n, obs, L, axes=axes, angles=angles, dtype=dtype, entangler=entangler, placement=placement,
                 device=dev)
     a = torch.as_tensor(angles, dtype=torch.float64, device=dev).reshape(-1)
     out = (torch.empty(1, dtype=torch.float64, device=dev), torch.empty(n * L, dtype=torch.float64, device=dev))
-    for _ in range(max(warmup, 3)):
+    for _ in range(max(warmup, min_warmup)):
         c.grad_run_tensors(a, out=out)
     torch.cuda.synchronize()
     e0, e1, st = _events(dev)
@@ -312,6 +315,8 @@ def measure_mcclean(n, L, seed, dtype, entangler, placement, steps, warmup, dev)
            "value": 1e3 / ms, "unit": "circuits/s", "ms_per_step": ms, "steps": steps,
            "hbm_gbs_algorithmic": B / ms * 1e-6, "hbm_frac_step": B / ms * 1e-6 / hbm,
            "hbm_peak_source": "MEASURED_PEAKS.json hbm_gbs"}
+    op = _native.choose_grad_op(c.native(), c._dtype_code, dev, c.grad_mode)
+    res["grad_mode"] = "history" if op == _lib.QG_OP_GRAD_HISTORY else "uncompute"
     c._native.release_workspaces()
     return res
 
@@ -795,6 +800,8 @@ def main():
             args.n, args.layers, args.seed, other, args.entangler, args.placement, 5, 3, dev)
         line["cz_after"] = measure_mcclean(args.n, args.layers, args.seed, args.dtype, "cz", "after", 5, 3, dev)
         line["qaoa"] = _public(measure_qaoa(24, 10, 24, "complex128", 5, 3, dev))
+        # the largest configured size whose history does not fit: uncompute mode
+        line["large"] = measure_mcclean(28, 50, 28, "complex128", "cnot", "before", 2, 2, dev, min_warmup=2)
         line["batched"] = measure_batched(14, 30, 4096, "complex64", 5, 3, 14, dev, e2e=True)
         line["served"] = {"small": measure_served(24, 1000, 14, args.streams, dev),
                           "full": measure_served(26, 60, 26, args.streams, dev)}
