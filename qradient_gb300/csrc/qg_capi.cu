@@ -133,11 +133,23 @@ int default_tile_bits(int dtype, int n) {
   return env_int("QG_TILE_BITS_C64", 12);
 }
 
+// Sweeps per layer with tA tile bits in sweep A and tB in the high-bit sweeps.
+int sweeps_per_layer2(int n, int tA, int tB, int c) {
+  return n <= tA ? 1 : 1 + (n - tA + (tB - c) - 1) / (tB - c);
+}
+
 Layout make_layout(int n, int dtype, int tile_bits) {
   Layout lay;
   int t = tile_bits > 0 ? tile_bits : default_tile_bits(dtype, n);
   const int c = dtype == QG_C128 ? 3 : 4;
   t = std::max(c + 2, std::min(t, max_tile_bits(dtype)));
+  // complex128 default with 12-bit tiles: the high-bit sweeps take 11 bits
+  // (the compile-time-size kernel, two CTAs per SM) where that costs no
+  // sweep per layer (n = 20 and 28); sweep A keeps its 12 bits
+  int tb = t;
+  if (tile_bits <= 0 && dtype == QG_C128 && t == 12 && env_int("QG_TILE_BITS_C128", 0) == 0 &&
+      sweeps_per_layer2(n, 12, 11, c) <= sweeps_per_layer(n, 12, c))
+    tb = 11;
   if (n <= t) {
     lay.t = n;
     std::vector<int> all;
@@ -153,9 +165,9 @@ Layout make_layout(int n, int dtype, int tile_bits) {
   lay.active.push_back(a);
   int next = t;
   while (next < n) {
-    const int k = std::min(t - c, n - next);
+    const int k = std::min(tb - c, n - next);
     std::vector<int> bits, act;
-    for (int b = 0; b < t - k; ++b) bits.push_back(b);
+    for (int b = 0; b < tb - k; ++b) bits.push_back(b);
     for (int i = 0; i < k; ++i) {
       bits.push_back(next + i);
       act.push_back(next + i);
@@ -450,7 +462,8 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
     // occupancy per distinct shared-memory footprint (phase-table size, cost table)
     std::vector<std::pair<int64_t, std::pair<int, int>>> memo;
     for (const auto& d : P.sweeps) {
-      const int64_t key = ((int64_t)d.nz << 32) | ((int64_t)(d.cost == COST_INT ? 1 : 0) << 31) | d.cost_maxabs;
+      const int64_t key = ((int64_t)d.t << 40) | ((int64_t)d.nz << 32) | ((int64_t)(d.cost == COST_INT ? 1 : 0) << 31) |
+                          d.cost_maxabs;
       int pf = -1, pb = -1;
       for (const auto& mm : memo)
         if (mm.first == key) {
@@ -469,8 +482,9 @@ WsLayout ws_layout(const qg_circuit* c, int dtype, int op, const Program& P) {
         }
         memo.push_back({key, {pf, pb}});
       }
-      w.grid_fwd_k.push_back((int)std::min<int64_t>(ntiles, (int64_t)sms * pf));
-      w.grid_bwd_k.push_back((int)std::min<int64_t>(ntiles, (int64_t)sms * pb));
+      const int64_t nt = (int64_t)1 << (n - d.t);  // this sweep's tiles (high-bit sweeps may be smaller)
+      w.grid_fwd_k.push_back((int)std::min<int64_t>(nt, (int64_t)sms * pf));
+      w.grid_bwd_k.push_back((int)std::min<int64_t>(nt, (int64_t)sms * pb));
     }
     for (int g : w.grid_bwd_k) w.G = std::max(w.G, g);
   }
