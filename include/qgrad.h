@@ -143,15 +143,19 @@ int qg_sample(int n, int dtype, const void* state_dev, int64_t nshots, uint64_t 
  * amplitudes in shared memory and applies every rotation on those bits in
  * one pass (the fusion depth); ctas_per_sm sets the persistent grid (block
  * shape across the SMs, capped at what fits).  0 restores the default
- * (tile_bits 11 for complex128, 12 for complex64; ctas_per_sm from the
- * occupancy query).  tile_bits: 5..12 for complex128, 6..13 for
+ * (tile_bits 11 for complex128, 12 for complex64; complex128 takes 12 for
+ * the first sweep of a layer where that saves a sweep per layer, with 11
+ * for the others where that costs none; ctas_per_sm from the
+ * occupancy query).  A non-zero tile_bits applies to every sweep.
+ * tile_bits: 5..12 for complex128, 6..13 for
  * complex64 (the backward sweep holds two tiles in shared memory); tiles
  * larger than the state use the whole state.  Call before launches that use the handle, not while
  * another thread uses it; the workspace size may change with the setting.
  * flags: QG_TUNE_FWD_PIPELINED or QG_TUNE_FWD_PLAIN choose the forward
  * sweep kernel (0: the default, pipelined).
- * qg_get_tuning reports the effective values (tile bits after clamping to
- * n, CTAs per SM of the backward sweeps, the forward kernel flag).  The autotuner of
+ * qg_get_tuning reports the effective values (tile bits of a layer's first
+ * sweep after clamping to n, CTAs per SM of the backward sweeps, the
+ * forward kernel flag).  The autotuner of
  * qradient_gb300/tuning.py picks them by timing. */
 enum {
   QG_TUNE_FWD_PIPELINED = 1, /* forward sweeps prefetch the next tile (double-buffered) */
