@@ -39,19 +39,6 @@ CLUSTER_MAX = {_lib.QG_C64: 14, _lib.QG_C128: 13}
 MAX_COST = 511
 
 
-def _to_device(host, device):
-    """Host array -> device tensor without synchronising the current stream:
-    staged through pinned memory (whose block the host allocator keeps until
-    the copy has run) and copied asynchronously in stream order.  A plain
-    copy from pageable memory would wait for all earlier work on the stream."""
-    return torch.from_numpy(host).pin_memory().to(device, non_blocking=True)
-
-
-def _dev_bytes(arr, device):
-    a = np.ascontiguousarray(arr)
-    return _to_device(a.view(np.uint8).reshape(-1).copy(), device)
-
-
 class Batch:
     """A fixed list of jobs executed together; parameters live in ``params``."""
 
@@ -71,6 +58,7 @@ class Batch:
         self._specs = []
         self._keep = []
         self._graph = None
+        self._views = None
         self.finalized = False
 
     # ------------------------------------------------------------ building
@@ -95,37 +83,56 @@ class Batch:
 
     def finalize(self):
         dev = self.device
-        total = sum(s["nparams"] for s in self._specs)
-        B = len(self._specs)
-        # initial parameters packed on the host and copied in one transfer
+        specs = self._specs
+        B = len(specs)
+        off = toff = 0
+        for sp in specs:
+            sp["off"] = off
+            off += sp["nparams"]
+            nt = sp["circuit"].observable.num_components if self.want_terms else 0
+            sp["toff"], sp["nterm"] = toff, nt
+            toff += nt
+        total = off
+        # initial parameters packed on the host; they travel with the batch's
+        # one host-to-device copy (_build_groups)
         host = np.zeros(max(total, 1), dtype=np.float64)
-        off = 0
-        for s in self._specs:
-            s["off"] = off
-            if s["init"] is not None:
-                init = s["init"]
+        for sp in specs:
+            init = sp["init"]
+            if init is not None:
                 if isinstance(init, torch.Tensor):
                     init = init.detach().cpu().numpy()
-                host[off: off + s["nparams"]] = np.asarray(init, dtype=np.float64).reshape(-1)
-            off += s["nparams"]
-        self.params_flat = _to_device(host, dev)
-        # every output slot is written by the kernels (a 2-CTA job clears its
-        # slots before adding to them), so no clearing is needed here
-        self.grads_flat = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
-        self.expec = torch.empty(max(B, 1), dtype=torch.float64, device=dev)
-        self.params = [self.params_flat[s["off"]: s["off"] + s["nparams"]] for s in self._specs]
-        self.grads = [self.grads_flat[s["off"]: s["off"] + s["nparams"]] for s in self._specs]
-        toff = 0
-        for s in self._specs:
-            s["toff"] = toff
-            toff += s["circuit"].observable.num_components if self.want_terms else 0
-        self.term_expec_flat = torch.empty(max(toff, 1), dtype=torch.float64, device=dev)
-        self.term_expec = [self.term_expec_flat[s["toff"]: s["toff"] + (s["circuit"].observable.num_components
-                                                                         if self.want_terms else 0)]
-                           for s in self._specs]
+                host[sp["off"]: sp["off"] + sp["nparams"]] = np.asarray(init, dtype=np.float64).reshape(-1)
+        # outputs in one allocation: gradients | expectation values | term
+        # expectations.  Every output slot is written by the kernels (a 2-CTA
+        # job clears its slots before adding to them): no clearing is needed.
+        ng, nb, ne = max(total, 1), max(B, 1), max(toff, 1)
+        out = torch.empty(ng + nb + ne, dtype=torch.float64, device=dev)
+        self.grads_flat, self.expec, self.term_expec_flat = out[:ng], out[ng:ng + nb], out[ng + nb:]
+        self._views = None
         self._structures = {}
-        self._build_groups()
+        self._build_groups(host)
         self.finalized = True
+
+    # per-job views of the flat buffers, made on first use
+    def _job_views(self):
+        if self._views is None:
+            sp = self._specs
+            self._views = ([self.params_flat[s["off"]: s["off"] + s["nparams"]] for s in sp],
+                           [self.grads_flat[s["off"]: s["off"] + s["nparams"]] for s in sp],
+                           [self.term_expec_flat[s["toff"]: s["toff"] + s["nterm"]] for s in sp])
+        return self._views
+
+    @property
+    def params(self):
+        return self._job_views()[0]
+
+    @property
+    def grads(self):
+        return self._job_views()[1]
+
+    @property
+    def term_expec(self):
+        return self._job_views()[2]
 
     def refinalize(self, cluster_from):
         """Regroup the jobs with a new cluster split; parameters are kept."""
@@ -134,97 +141,123 @@ class Batch:
             return self.finalize()
         self.cluster_from = int(cluster_from)
         self._graph = None
-        self._build_groups()
+        self._build_groups(None)
 
-    def _build_groups(self):
+    def _build_groups(self, host_params):
+        """Job tables per launch group.  Everything the batch uploads -- the
+        initial parameters (host_params; None keeps the device ones), the
+        structure arrays of circuits not uploaded yet, the job tables and
+        the groups' job counters -- is packed into one host buffer and
+        copied to one device allocation in a single asynchronous transfer."""
         dev = self.device
-        # shared structure buffers, one per distinct circuit object, packed
-        # into one device blob (one host-to-device copy for the batch)
         cache = self._structures
-        self._upload_structures()
-        single, cmax = SINGLE_MAX[self.dtype], CLUSTER_MAX[self.dtype]
-        split = max(4, min(self.cluster_from, single + 1))
-        # job tables filled column by column (one numpy assignment per field)
-        cols = {k: [] for k in ("i", "kind", "n", "layers", "entangler", "placement", "nterms", "terms", "axes",
-                                "cost_nterms", "cost_maxabs", "cost_w0", "cost", "periodic")}
-        big = []
-        for i, s in enumerate(self._specs):
-            c = s["circuit"]
-            st = cache[id(c)]
-            # the periodic ladder targets the top qubit, which a 2-CTA job splits
-            periodic = s["kind"] == 0 and c.entangler == "cnot_periodic"
-            if c.qnum > cmax or st is None or (periodic and c.qnum > single):
-                big.append(i)
-                continue
-            mc = s["kind"] == 0
-            for k, v in (("i", i), ("kind", s["kind"]), ("n", c.qnum), ("layers", c.lnum),
-                         ("entangler", _ENT[c.entangler] if mc else 0), ("placement", _PLACE[c.placement] if mc else 0),
-                         ("nterms", st["nterms"]), ("terms", st["terms"]), ("axes", st["axes"]),
-                         ("cost_nterms", st["cost_nterms"]), ("cost_maxabs", st["cost_maxabs"]),
-                         ("cost_w0", st["cost_w0"]), ("cost", st["cost"]), ("periodic", periodic)):
-                cols[k].append(v)
-        idx = np.asarray(cols["i"], dtype=np.int64)
-        qn = np.asarray(cols["n"], dtype=np.int64)
-        offs = np.asarray([self._specs[i]["off"] for i in idx], dtype=np.uint64)
-        toffs = np.asarray([self._specs[i]["toff"] for i in idx], dtype=np.uint64)
-        pbase, gbase, ebase = self.params_flat.data_ptr(), self.grads_flat.data_ptr(), self.expec.data_ptr()
-        tbase = self.term_expec_flat.data_ptr()
-        self._groups = []
-        per = np.asarray(cols["periodic"], dtype=bool)
-        for cl, sel in ((1, (qn < split) | per), (2, (qn >= split) & ~per)):
-            nj = int(sel.sum())
-            if nj == 0:
-                continue
-            arr = np.zeros(nj, dtype=_JOB)
-            for k in ("kind", "n", "layers", "entangler", "placement", "nterms", "terms", "axes", "cost_nterms",
-                      "cost_maxabs", "cost_w0", "cost"):
-                arr[k] = np.asarray(cols[k])[sel]
-            arr["params"] = pbase + 8 * offs[sel]
-            arr["expec"] = ebase + 8 * idx[sel].astype(np.uint64)
-            arr["grad"] = gbase + 8 * offs[sel] if self.want_grad else 0
-            arr["term_expec"] = tbase + 8 * toffs[sel] if self.want_terms else 0
-            maxq = int(qn[sel].max())
-            ws = torch.empty(256, dtype=torch.uint8, device=dev)  # job counter, cleared by qg_batch_launch
-            self._groups.append((cl, _dev_bytes(arr, dev), nj, maxq, ws))
-        self._big = big
-
-    def _upload_structures(self):
-        """Host arrays of every circuit not yet uploaded, packed 16-byte
-        aligned into one buffer and copied to the device at once; the cache
-        then holds device addresses."""
-        pending, blobs, size, seen = [], [], 0, set()
-        for s in self._specs:
-            c = s["circuit"]
-            if id(c) in self._structures or id(c) in seen:
+        # structure arrays of new circuits, at offsets relative to their region
+        pending, blobs, ssize, seen = [], [], 0, set()
+        for sp in self._specs:
+            c = sp["circuit"]
+            if id(c) in cache or id(c) in seen:
                 continue
             seen.add(id(c))
-            st = self._structure(c, s["kind"])
+            st = self._structure(c, sp["kind"])
             if st is None:
-                self._structures[id(c)] = None  # runs on the sweep path
+                cache[id(c)] = None  # runs on the sweep path
                 continue
-            offs = {}
+            rel = {}
             for key in ("terms", "axes", "cost"):
                 a = st[key]
                 if a is None:
                     continue
                 b = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
-                size = (size + 15) & ~15
-                offs[key] = size
-                blobs.append((size, b))
-                size += b.size
-            pending.append((c, st, offs))
-        if not pending:
-            return
-        host = np.zeros(max(size, 16), dtype=np.uint8)
+                ssize = (ssize + 15) & ~15
+                rel[key] = ssize
+                blobs.append((ssize, b))
+                ssize += b.size
+            pending.append((c, st, rel))
+            cache[id(c)] = st
+        single, cmax = SINGLE_MAX[self.dtype], CLUSTER_MAX[self.dtype]
+        split = max(4, min(self.cluster_from, single + 1))
+        # job rows, one list per field
+        cols = {k: [] for k in ("i", "kind", "n", "layers", "entangler", "placement", "st", "periodic")}
+        big = []
+        for i, sp in enumerate(self._specs):
+            c = sp["circuit"]
+            st = cache[id(c)]
+            # the periodic ladder targets the top qubit, which a 2-CTA job splits
+            periodic = sp["kind"] == 0 and c.entangler == "cnot_periodic"
+            if c.qnum > cmax or st is None or (periodic and c.qnum > single):
+                big.append(i)
+                continue
+            mc = sp["kind"] == 0
+            cols["i"].append(i)
+            cols["kind"].append(sp["kind"])
+            cols["n"].append(c.qnum)
+            cols["layers"].append(c.lnum)
+            cols["entangler"].append(_ENT[c.entangler] if mc else 0)
+            cols["placement"].append(_PLACE[c.placement] if mc else 0)
+            cols["st"].append(st)
+            cols["periodic"].append(periodic)
+        idx = np.asarray(cols["i"], dtype=np.int64)
+        qn = np.asarray(cols["n"], dtype=np.int64)
+        per = np.asarray(cols["periodic"], dtype=bool)
+        groups = []
+        for cl, sel in ((1, (qn < split) | per), (2, (qn >= split) & ~per)):
+            nj = int(sel.sum()) if idx.size else 0
+            if nj:
+                groups.append((cl, sel, nj, int(qn[sel].max())))
+        # layout of the upload: params | structures | job tables | job counters
+        size = 0
+        p_off = None
+        if host_params is not None:
+            p_off, size = 0, host_params.nbytes
+        size = (size + 15) & ~15
+        s_off = size
+        size += ssize
+        j_offs = []
+        for cl, sel, nj, maxq in groups:
+            size = (size + 15) & ~15
+            j_offs.append(size)
+            size += nj * _JOB.itemsize
+        c_offs = []
+        for _ in groups:
+            size = (size + 255) & ~255
+            c_offs.append(size)  # job counter, cleared by qg_batch_launch
+            size += 256
+        size = max((size + 15) & ~15, 16)
+        blob = torch.empty(size, dtype=torch.uint8, device=dev)
+        base = blob.data_ptr()
+        host = np.zeros(size, dtype=np.uint8)
+        if host_params is not None:
+            host[p_off: p_off + host_params.nbytes] = host_params.view(np.uint8)
+            self.params_flat = blob[p_off: p_off + host_params.nbytes].view(torch.float64)
         for o, b in blobs:
-            host[o:o + b.size] = b
-        buf = _to_device(host, self.device)
-        self._blobs = getattr(self, "_blobs", []) + [buf]
-        base = buf.data_ptr()
-        for c, st, offs in pending:
+            host[s_off + o: s_off + o + b.size] = b
+        for c, st, rel in pending:
             for key in ("terms", "axes", "cost"):
-                st[key] = base + offs[key] if key in offs else 0
-            self._structures[id(c)] = st
+                st[key] = base + s_off + rel[key] if key in rel else 0
+        offs = np.asarray([self._specs[i]["off"] for i in idx], dtype=np.uint64)
+        toffs = np.asarray([self._specs[i]["toff"] for i in idx], dtype=np.uint64)
+        pbase, gbase, ebase = self.params_flat.data_ptr(), self.grads_flat.data_ptr(), self.expec.data_ptr()
+        tbase = self.term_expec_flat.data_ptr()
+        sts = cols["st"]
+        self._groups = []
+        for (cl, sel, nj, maxq), jo, co in zip(groups, j_offs, c_offs):
+            arr = np.zeros(nj, dtype=_JOB)
+            for k in ("kind", "n", "layers", "entangler", "placement"):
+                arr[k] = np.asarray(cols[k])[sel]
+            ssel = [st for st, m in zip(sts, sel) if m]
+            for k in ("nterms", "terms", "axes", "cost_nterms", "cost_maxabs", "cost_w0", "cost"):
+                arr[k] = [st[k] for st in ssel]
+            arr["params"] = pbase + 8 * offs[sel]
+            arr["expec"] = ebase + 8 * idx[sel].astype(np.uint64)
+            arr["grad"] = gbase + 8 * offs[sel] if self.want_grad else 0
+            arr["term_expec"] = tbase + 8 * toffs[sel] if self.want_terms else 0
+            host[jo: jo + arr.nbytes] = arr.view(np.uint8)
+            self._groups.append((cl, blob[jo: jo + arr.nbytes], nj, maxq, blob[co: co + 256]))
+        # one asynchronous copy in stream order, staged through pinned memory
+        # (whose block the host allocator keeps until the copy has run)
+        blob.copy_(torch.from_numpy(host).pin_memory(), non_blocking=True)
+        self._blobs = getattr(self, "_blobs", []) + [blob]
+        self._big = big
 
     def _structure(self, c, kind):
         """Host-side structure arrays of one circuit (uploaded by the caller)."""

@@ -245,7 +245,9 @@ class Server:
         try:
             nat = r.circuit.native()
             with torch.cuda.stream(st):
-                params = torch.as_tensor(r.params.reshape(-1)).to(self.device, non_blocking=False)
+                # asynchronous in stream order, staged through pinned memory
+                params = torch.from_numpy(np.ascontiguousarray(r.params.reshape(-1))).pin_memory().to(
+                    self.device, non_blocking=True)
                 if r.op == "grad":
                     ws = nat.workspace(r.dtype, _lib.QG_OP_GRAD_UNCOMPUTE, self.device)
                     e, g = nat.grad(params, r.dtype, self.device, _lib.QG_OP_GRAD_UNCOMPUTE, workspace=ws)
