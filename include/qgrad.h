@@ -284,11 +284,6 @@ int qg_batch_launch(int dtype, const qg_batch_job* jobs_dev, int njobs, int max_
 int qg_grad_noalloc(const qg_circuit* c, int dtype, const double* params_dev, const void* ini_state_dev,
                     double* expec_dev, double* grad_dev, qg_stream stream);
 
-/* Measured FP64 FMA issue rate of this GPU (FMA/s), for roofline
- * reporting: a dependent-chain DFMA kernel timed with CUDA events.
- * scratch_dev needs 1 MiB.  Synchronises the stream. */
-int qg_probe_fp64_fma_rate(void* scratch_dev, size_t scratch_bytes, double* fma_per_s, qg_stream stream);
-
 /* Launch timing for roofline reporting.  While enabled, the library records
  * a CUDA event pair (on the launching stream) around every sweep launch of
  * the calling thread; qg_profile_collect waits for them and returns the

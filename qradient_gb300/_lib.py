@@ -34,7 +34,6 @@ SIGNATURES = {
     "qg_maxcut_table": (_I, [_I, _I, _P, _P, _P]),
     "qg_sample_workspace_size": (_I, [_I, ctypes.POINTER(_SZ)]),
     "qg_sample": (_I, [_I, _I, _P, _I64, _U64, _U64, _P, _SZ, _P, _P]),
-    "qg_probe_fp64_fma_rate": (_I, [_P, _SZ, ctypes.POINTER(ctypes.c_double), _P]),
     "qg_qaoa_cost_terms": (_I, [_I, _I, _P, _P, _P, _P, _I, _P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(_I)]),
     "qg_batch_workspace_size": (_I, [ctypes.POINTER(_SZ)]),

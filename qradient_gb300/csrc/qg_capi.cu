@@ -1216,10 +1216,4 @@ int qg_batch_launch(int dtype, const qg_batch_job* jobs, int njobs, int max_qubi
   return QG_OK;
 }
 
-int qg_probe_fp64_fma_rate(void* scratch, size_t bytes, double* rate, qg_stream stream) {
-  if (!scratch || !rate) return fail(QG_ERR_INVALID, "null pointer");
-  QG_CUDA(probe_fp64((double*)scratch, bytes, rate, (cudaStream_t)stream));
-  return QG_OK;
-}
-
 }  // extern "C"

@@ -1,4 +1,4 @@
-// Cost tables, the shot sampler and the FP64 rate probe.
+// Cost tables and the shot sampler.
 #include <stdint.h>
 
 #include "qg_extra.h"
@@ -166,62 +166,5 @@ template cudaError_t launch_sample<double2>(int, const double2*, int64_t, uint64
                                             cudaStream_t);
 template cudaError_t launch_sample<float2>(int, const float2*, int64_t, uint64_t, uint64_t, double*, int64_t*,
                                            cudaStream_t);
-
-// ------------------------------------------------------------ FP64 probe
-
-// 16 independent FMA chains per thread, enough to cover the FP64 pipe latency
-__global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
-  double x[16];
-#pragma unroll
-  for (int c = 0; c < 16; ++c) x[c] = threadIdx.x * 1e-3 + c;
-  for (int i = 0; i < iters; ++i) {
-#pragma unroll
-    for (int c = 0; c < 16; ++c) x[c] = fma(x[c], a, b);
-  }
-  double s = 0.0;
-#pragma unroll
-  for (int c = 0; c < 16; ++c) s += x[c];
-  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-
-cudaError_t probe_fp64(double* scratch, size_t bytes, double* rate, cudaStream_t st) {
-  int dev = 0, sms = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  const int threads = 256;
-  // exactly one wave of resident blocks: a partial second wave would leave
-  // SMs idle at the end and understate the rate
-  int per = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfma_probe_kernel, threads, 0);
-  if (e != cudaSuccess) return e;
-  int blocks = sms * (per > 0 ? per : 1);
-  if ((size_t)blocks * threads * sizeof(double) > bytes) blocks = (int)(bytes / (threads * sizeof(double)));
-  if (blocks < 1) return cudaErrorInvalidValue;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  const int iters = 4096;
-  dfma_probe_kernel<<<blocks, threads, 0, st>>>(scratch, 64, 1.0000001, 1e-9);
-  double best = 0.0;
-  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
-    cudaEventRecord(e0, st);
-    dfma_probe_kernel<<<blocks, threads, 0, st>>>(scratch, iters, 1.0000001, 1e-9);
-    cudaEventRecord(e1, st);
-    e = cudaEventSynchronize(e1);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-    if (e == cudaSuccess && ms > 0.f) {
-      const double r = (double)blocks * threads * iters * 16.0 / (ms * 1e-3);
-      if (r > best) best = r;
-    }
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (e != cudaSuccess) return e;
-  *rate = best;
-  return cudaGetLastError();
-}
 
 }  // namespace qg

@@ -1,4 +1,4 @@
-// Cost tables, sampler and FP64 probe (qg_extra.cu).
+// Cost tables and the sampler (qg_extra.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -37,7 +37,5 @@ cudaError_t launch_real_cost(int n, const RealTermList& terms, double* table, in
 template <typename C>
 cudaError_t launch_sample(int n, const C* psi, int64_t nshots, uint64_t seed, uint64_t offset, double* ws,
                           int64_t* out, cudaStream_t st);
-
-cudaError_t probe_fp64(double* scratch, size_t bytes, double* rate, cudaStream_t st);
 
 }  // namespace qg
