@@ -6,10 +6,12 @@ dtype) arrive over time.  Each scheduling round:
 1. completed work is retired: results copied to the host, latency recorded,
    its device memory returned to the admission budget;
 2. queued requests are admitted in arrival order while their device
-   footprint fits the budget (an adjoint request needs its workspace: psi and
-   lambda, doubled when the CNOT ladder needs ping-pong buffers; requests
-   that fit the shared-memory kernel need only their parameters and
-   outputs);
+   footprint fits the budget (an adjoint request on the sweep path needs
+   its workspace: the stored state history where that takes at most
+   ``history_share`` of the budget -- the faster form, as ``grad_run``'s
+   default picks it -- else the uncompute form's psi and lambda, doubled
+   when the CNOT ladder needs ping-pong buffers; requests that fit the
+   shared-memory kernel need only their parameters and outputs);
 3. admitted small requests are packed into one batched persistent launch
    (``qg_batch_launch``) on the next of a few batch streams, each admitted
    large request gets its own stream running the sweep kernels.  Work from
@@ -39,7 +41,7 @@ from .batched import CLUSTER_MAX, Batch
 
 class Request:
     __slots__ = ("rid", "circuit", "params", "op", "dtype", "t_arrival", "t_done", "expec", "grad", "state",
-                 "footprint", "error", "_e", "_g", "_event", "_keep")
+                 "footprint", "error", "_e", "_g", "_event", "_keep", "_gop")
 
     def __init__(self, rid, circuit, params, op="grad", dtype="complex128", t_arrival=None):
         self.rid = rid
@@ -58,6 +60,7 @@ class Request:
         self._e = self._g = None
         self._event = None
         self._keep = None
+        self._gop = None
 
     @property
     def latency(self):
@@ -80,12 +83,14 @@ class Server:
     """Admission by device-memory footprint, batched small requests, one
     stream per large request (up to ``streams`` concurrently)."""
 
-    def __init__(self, device=None, hbm_budget=None, streams=8, max_batch=4096, batch_streams=4):
+    def __init__(self, device=None, hbm_budget=None, streams=8, max_batch=4096, batch_streams=4,
+                 history_share=0.5):
         self.device = _native.require_cuda(device)
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info(self.device)
             hbm_budget = int(0.5 * free)
         self.budget = int(hbm_budget)
+        self.history_share = float(history_share)
         self.in_use = 0
         self.max_batch = max_batch
         self.queue = collections.deque()
@@ -161,8 +166,18 @@ class Server:
             np_ = r.params.size
             r.footprint = 8 * (2 * np_ + 1) + 4096
         else:
-            op = _lib.QG_OP_GRAD_UNCOMPUTE if r.op == "grad" else _lib.QG_OP_RUN
-            r.footprint = r.circuit.native().workspace_bytes(r.dtype, op) + 8 * (2 * r.params.size + 1)
+            nat = r.circuit.native()
+            if r.op == "grad":
+                op = _lib.QG_OP_GRAD_HISTORY
+                ws = nat.workspace_bytes(r.dtype, op)
+                if ws > self.history_share * self.budget:
+                    op = _lib.QG_OP_GRAD_UNCOMPUTE
+                    ws = nat.workspace_bytes(r.dtype, op)
+            else:
+                op = _lib.QG_OP_RUN
+                ws = nat.workspace_bytes(r.dtype, op)
+            r._gop = op
+            r.footprint = ws + 8 * (2 * r.params.size + 1)
 
     # ------------------------------------------------------------ scheduling
     def _retire(self):
@@ -249,8 +264,8 @@ class Server:
                 params = torch.from_numpy(np.ascontiguousarray(r.params.reshape(-1))).pin_memory().to(
                     self.device, non_blocking=True)
                 if r.op == "grad":
-                    ws = nat.workspace(r.dtype, _lib.QG_OP_GRAD_UNCOMPUTE, self.device)
-                    e, g = nat.grad(params, r.dtype, self.device, _lib.QG_OP_GRAD_UNCOMPUTE, workspace=ws)
+                    ws = nat.workspace(r.dtype, r._gop, self.device)
+                    e, g = nat.grad(params, r.dtype, self.device, r._gop, workspace=ws)
                 else:
                     ws = nat.workspace(r.dtype, _lib.QG_OP_RUN, self.device)
                     e, _ = nat.run(params, r.dtype, self.device, workspace=ws)
