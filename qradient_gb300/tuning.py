@@ -85,13 +85,15 @@ def get_tuning(native, dtype):
 
 
 def sweep_candidates(dtype, n):
-    """(tile_bits, ctas_per_sm, flags) triples: three fusion depths around
-    the default, each at the occupancy-sized grid and at 1 CTA per SM, with
-    plain and with pipelined (double-buffered) forward sweeps."""
+    """(tile_bits, ctas_per_sm, flags) triples: the default plan (tile_bits
+    0: the library's per-sweep tile sizes), then three uniform fusion depths
+    around the default, each at the occupancy-sized grid and at 1 CTA per
+    SM, with plain and with pipelined (double-buffered) forward sweeps."""
     depths = (10, 11, 12) if dtype == _lib.QG_C128 else (11, 12, 13)
     lo = 5 if dtype == _lib.QG_C128 else 6
     depths = sorted({max(lo, min(t, n)) for t in depths})
-    return [(t, c, f) for t in depths for c in (0, 1) for f in (_lib.QG_TUNE_FWD_PLAIN, _lib.QG_TUNE_FWD_PIPELINED)]
+    return [(0, 0, 0)] + [(t, c, f) for t in depths for c in (0, 1)
+                          for f in (_lib.QG_TUNE_FWD_PLAIN, _lib.QG_TUNE_FWD_PIPELINED)]
 
 
 def _time_ms(fn, reps):

@@ -68,7 +68,12 @@ def test_tuner_picks_applies_and_caches(golden, tmp_path, monkeypatch):
     assert len(r["timings"]) == len(tuning.sweep_candidates(circ._dtype_code, 16))
     assert all(t["ms"] > 0 for t in r["timings"])
     t_eff, _, f_eff = tuning.get_tuning(circ.native(), circ._dtype_code)
-    assert t_eff == min(r["tile_bits"], 16) and f_eff == r["flags"]
+    if r["tile_bits"] == 0:
+        # the default plan: the same effective values as an untuned circuit
+        fresh, _ = _golden_circuit(golden, "chain_n16_L50", "complex128")
+        assert (t_eff, f_eff) == tuple(tuning.get_tuning(fresh.native(), fresh._dtype_code)[::2])
+    else:
+        assert t_eff == min(r["tile_bits"], 16) and f_eff == r["flags"]
     data = json.load(open(tmp_path / "tune.json"))
     assert len(data) == 1
     # a second circuit of the same shape takes the cached choice without timing
