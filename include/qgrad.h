@@ -218,8 +218,8 @@ int qg_plateau_step(double* params_dev, const double* grad_dev, int nparams, con
 /* ---- Batched persistent execution (no reference counterpart: the
  * reference runs one circuit per Python call).  Many small circuits, each
  * a whole run or grad_run with psi and lambda resident in shared memory,
- * in one launch (CUDA-graph capturable).  Limits: complex64 n <= 14,
- * complex128 n <= 13, L <= 4096, and for QAOA an integer cost with
+ * in one launch (CUDA-graph capturable).  Limits: complex64 n <= 15,
+ * complex128 n <= 14, L <= 4096, and for QAOA an integer cost with
  * |m| <= 511. */
 typedef struct qg_term {
   int32_t kind, q0, q1, pad; /* qg_pauli, qubits (q1 for ZZ) */
@@ -262,7 +262,10 @@ int qg_batch_workspace_size(size_t* bytes);
 
 /* Run njobs jobs (jobs_dev: device array) in persistent launches.  All jobs
  * must share dtype; max_qubits bounds their n (sets the shared-memory size).
- * Jobs with n above the single-CTA limit use 2-CTA clusters. */
+ * cluster: CTAs per job, 1, 2 or 4 (the state split by its top 0, 1 or 2
+ * bits): one CTA holds complex64 n <= 13 / complex128 n <= 12, two one
+ * qubit more, four two more.  4-CTA jobs add their partial sums with atomic
+ * adds in arrival order (their outputs can vary in the last bit). */
 int qg_batch_launch(int dtype, const qg_batch_job* jobs_dev, int njobs, int max_qubits, int cluster,
                     void* workspace_dev, size_t workspace_bytes, qg_stream stream);
 

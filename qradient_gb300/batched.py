@@ -33,9 +33,11 @@ _ENT = {"cnot": _lib.QG_ENT_CNOT_LADDER, "cz": _lib.QG_ENT_CZ_LADDER, None: _lib
         "none": _lib.QG_ENT_NONE, "cnot_periodic": _lib.QG_ENT_CNOT_LADDER_PERIODIC}
 _PLACE = {"before": _lib.QG_PLACE_BEFORE, "after": _lib.QG_PLACE_AFTER}
 
-# largest qubit count held by one CTA / by a 2-CTA cluster
+# largest qubit count held by one CTA / a 2-CTA cluster / the batched kernel
+# (4-CTA clusters above the pair limit)
 SINGLE_MAX = {_lib.QG_C64: 13, _lib.QG_C128: 12}
-CLUSTER_MAX = {_lib.QG_C64: 14, _lib.QG_C128: 13}
+PAIR_MAX = {_lib.QG_C64: 14, _lib.QG_C128: 13}
+CLUSTER_MAX = {_lib.QG_C64: 15, _lib.QG_C128: 14}
 MAX_COST = 511
 
 
@@ -200,7 +202,8 @@ class Batch:
         qn = np.asarray(cols["n"], dtype=np.int64)
         per = np.asarray(cols["periodic"], dtype=bool)
         groups = []
-        for cl, sel in ((1, (qn < split) | per), (2, (qn >= split) & ~per)):
+        pair = PAIR_MAX[self.dtype]
+        for cl, sel in ((1, (qn < split) | per), (2, (qn >= split) & (qn <= pair) & ~per), (4, (qn > pair) & ~per)):
             nj = int(sel.sum()) if idx.size else 0
             if nj:
                 groups.append((cl, sel, nj, int(qn[sel].max())))

@@ -5,11 +5,13 @@
 // qaoa.py:23-70) executed with psi and lambda resident in shared memory:
 // no state ever goes to HBM.  A CTA holds the whole state when it fits
 // (complex64 n <= 13, complex128 n <= 12); a 2-CTA cluster holds one state
-// split by its top bit (qubit 0) otherwise (complex64 n = 14, complex128
-// n = 13), and the only cross-CTA operations (rotations, reductions and X/Y
-// observable terms on qubit 0) read the partner CTA's shared memory
-// (distributed shared memory) between cluster barriers.  The CNOT ladder
-// never targets qubit 0, so it stays inside each CTA.
+// split by its top bit (qubit 0) at the next size (complex64 n = 14,
+// complex128 n = 13) and a 4-CTA cluster, split by its top two bits, at the
+// one after (complex64 n = 15, complex128 n = 14).  The only cross-CTA
+// operations (rotations, reductions and X/Y observable terms on the split
+// qubits) read the partner CTA's shared memory (distributed shared memory)
+// between cluster barriers.  The CNOT ladder never targets qubit 0; its
+// CNOT(0, 1) permutes the 4-CTA blocks, which the CTAs follow by relabelling.
 //
 // Clusters (or CTAs) take jobs from a device counter until the queue is
 // empty (persistent grid, one launch per precision and cluster size; the
@@ -353,8 +355,8 @@ struct BShared {
   T xu[BMAXQ];
   T xk[BMAXQ];               // scale factor kappa of each X/Y rotation (scaled form = rotation / kappa)
   int xform[BMAXQ];
-  int caxis, cform, cslot;   // the cross rotation on the top bit (clusters)
-  T cu;
+  int caxis[2], cform[2], cslot[2], cbit[2];  // rotations on the cluster-split top bits (cbit: rank bit)
+  T cu[2];
   int zbit[BMAXQ];           // global bits of the Z rotations
   int zslot[BMAXQ];
   T zs[BMAXQ], zc[BMAXQ];
@@ -383,11 +385,22 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
   C* ztab = buf0 + 3 * Mmax;          // BATCH_TABLE entries: Z-rotation phases or QAOA cost phases
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = CS > 1 ? (int)cluster.block_rank() : 0;
+  constexpr int LGCS = CS == 4 ? 2 : CS == 2 ? 1 : 0;
   C* psi = buf0;
   C* lam = buf0 + Mmax;
   C* scr = buf0 + 2 * Mmax;
-  // the partner CTA's buffer with the same role (same offset)
-  auto remote = [&](C* v) -> C* { return CS > 1 ? cluster.map_shared_rank(v, rank ^ 1) : v; };
+  // The state is split by its top LGCS bits: this CTA holds the block whose
+  // top bits are its logical rank.  With 4 CTAs the CNOT ladder's CNOT(0, 1)
+  // (control and target both top bits) permutes whole blocks: h(t) = t ^
+  // (t >> 1 & 1) in both directions, an involution.  Instead of moving the
+  // blocks, every CTA relabels (hflip): logical rank h(rank) while hflip is
+  // set, and the CTA holding logical block l is h(l).  2-CTA clusters keep
+  // the identity (the ladder never targets qubit 0).
+  int hflip = 0;
+  auto hmap = [](int t) { return t ^ ((t >> 1) & 1); };
+  auto phys = [&](int l) { return CS == 4 && hflip ? hmap(l) : l; };
+  // the buffer with the same role (same offset) in the CTA holding logical block l
+  auto rmt = [&](C* v, int l) -> C* { return CS > 1 ? cluster.map_shared_rank(v, phys(l)) : v; };
   auto csync = [&]() {
     if (CS > 1)
       cluster.sync();
@@ -399,7 +412,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     if (tid == 0 && rank == 0) {
       const int j = atomicAdd(counter, 1);
       S.job = j;
-      if (CS > 1) *cluster.map_shared_rank(&S.job, 1) = j;
+      for (int r = 1; r < CS; ++r) *cluster.map_shared_rank(&S.job, r) = j;
     }
     csync();
     const int jid = S.job;
@@ -409,9 +422,19 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     lam = buf0 + Mmax;
     scr = buf0 + 2 * Mmax;
     const int n = J.n;
-    const int m = n - (CS > 1 ? 1 : 0);
+    const int m = n - LGCS;
     const int M = 1 << m;
-    const uint32_t top = (uint32_t)rank << m;
+    hflip = 0;
+    int lrank = rank;  // logical rank: the top bits of this CTA's block
+    uint32_t top = (uint32_t)lrank << m;
+    // the open CNOT ladder's block permutation (4-CTA jobs), before a gather
+    auto relabel = [&]() {
+      if (CS == 4) {
+        hflip ^= 1;
+        lrank = hmap(lrank);
+        top = (uint32_t)lrank << m;
+      }
+    };
     const bool grad = J.grad != nullptr;
     const int L = J.layers;
     uint32_t lodd = 0, leven = 0;
@@ -486,7 +509,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         const int b = n - 1 - q;
         const int slot = J.kind == 0 ? i * n + q : 2 * i;
         const bool isz = valid && axis == 2;
-        const bool iscross = valid && !isz && CS > 1 && b == m;
+        const bool iscross = valid && !isz && CS > 1 && b >= m;
         const bool isxy = valid && !isz && !iscross;
         int f = 0;
         R k = (R)1, u = (R)0, zs = (R)0, zc = (R)1;
@@ -510,21 +533,23 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           S.zs[idx] = zs;
           S.zc[idx] = zc;
         }
+        const unsigned mc = __ballot_sync(full, iscross);
         if (iscross) {
-          S.caxis = axis;
-          S.cslot = slot;
-          S.cu = u;
-          S.cform = f;
+          const int idx = __popc(mc & above);
+          S.caxis[idx] = axis;
+          S.cslot[idx] = slot;
+          S.cu[idx] = u;
+          S.cform[idx] = f;
+          S.cbit[idx] = b - m;
         }
         R kk = (isxy || iscross) ? k : (R)1;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) kk *= __shfl_xor_sync(full, kk, o);
-        const unsigned mc = __ballot_sync(full, iscross);
         if (lane == 0) {
           S.K = kk;
           S.nxy = __popc(mxy);
           S.nz = __popc(mz);
-          S.ncross = mc != 0u;
+          S.ncross = __popc(mc);
         }
       }
       __syncthreads();
@@ -650,20 +675,23 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     // in the other CTA; new values go to the scratch buffer, which then
     // becomes the rotated buffer
     auto rotate_cross = [&](C*& v, C*& v2, bool inverse) {
-      if (CS > 1 && S.ncross) {
+      const int nc = CS > 1 ? S.ncross : 0;
+      for (int c = 0; c < nc; ++c) {
+        const int cb = S.cbit[c];
+        const bool low = ((lrank >> cb) & 1) == 0;  // this block holds the bit-0 half
         for (int pass = 0; pass < (v2 ? 2 : 1); ++pass) {
           C*& w = pass ? v2 : v;
           cluster.sync();
-          const C* rw = remote(w);
+          const C* rw = rmt(w, lrank ^ (1 << cb));
           for (int e = tid; e < M; e += NT) {
             const C own = w[swb(e, DBL)];
             const C rem = rw[swb(e, DBL)];
-            C x0 = rank == 0 ? own : rem, x1 = rank == 0 ? rem : own;
+            C x0 = low ? own : rem, x1 = low ? rem : own;
             if (inverse)
-              rotp<-1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
+              rotp<-1, C, R>(x0, x1, S.caxis[c], S.cform[c], (R)S.cu[c]);
             else
-              rotp<1, C, R>(x0, x1, S.caxis, S.cform, (R)S.cu);
-            scr[swb(e, DBL)] = rank == 0 ? x0 : x1;
+              rotp<1, C, R>(x0, x1, S.caxis[c], S.cform[c], (R)S.cu[c]);
+            scr[swb(e, DBL)] = low ? x0 : x1;
           }
           cluster.sync();
           C* t = w;
@@ -753,20 +781,29 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       scr = t;
     };
 
-    // ---- forward
+    // ---- forward (relabel: the CNOT ladder's block permutation, before
+    // anything that reads the new block's index)
+    const bool ladder = J.kind == 0 && J.entangler == 1;
     for (int i = 0; i < L; ++i) {
       setup_layer(i, 1);
       if (fuse && S.nz <= BZMAX) {
+        if (ladder) relabel();
         build_diag(i, false);
         entangle_diag(psi, false);
       } else {
-        if (fuse) entangle(psi, false);
+        if (fuse) {
+          if (ladder) relabel();
+          entangle(psi, false);
+        }
         build_diag(i, false);
         apply_diag(psi, false);
       }
       if (CS > 1) cluster.sync();
       rotate(psi, nullptr, false);
-      if (J.kind == 0 && J.entangler != 0 && J.placement == 1) entangle(psi, false);
+      if (J.kind == 0 && J.entangler != 0 && J.placement == 1) {
+        if (ladder) relabel();
+        entangle(psi, false);
+      }
     }
     if (CS > 1) cluster.sync();
 
@@ -797,7 +834,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
               const uint32_t xp = x ^ b0;
               C u;
               if ((xp >> m) != (x >> m))
-                u = remote(psi)[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
+                u = rmt(psi, (int)(xp >> m))[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
               else
                 u = psi[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
               const R w = tw;
@@ -851,7 +888,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
             acc += sg ? -p2 : p2;
           } else {
             const uint32_t xp = x ^ b0;
-            const C u = (xp >> m) != (x >> m) ? remote(psi)[swb((int)(xp & (uint32_t)(M - 1)), DBL)]
+            const C u = (xp >> m) != (x >> m) ? rmt(psi, (int)(xp >> m))[swb((int)(xp & (uint32_t)(M - 1)), DBL)]
                                               : psi[swb((int)(xp & (uint32_t)(M - 1)), DBL)];
             if (t.kind == 0) {
               acc += fma(v.x, u.x, v.y * u.y);  // Re(conj(v) u)
@@ -883,6 +920,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
       for (int i = L - 1; i >= 0; --i) {
         setup_layer(i, -1);
         if (J.kind == 0 && J.entangler != 0 && J.placement == 1) {
+          if (ladder) relabel();
           entangle(psi, true);
           entangle(lam, true);
           if (CS > 1) cluster.sync();
@@ -921,17 +959,20 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           __syncthreads();
         }
         int ns = nxy;
-        if (CS > 1 && S.ncross) {
-          cluster.sync();  // the partner's psi has its local rotations applied
+        const int ncr = CS > 1 ? S.ncross : 0;
+        if (ncr) cluster.sync();  // the partners' psi has its local rotations applied
+        for (int c = 0; c < ncr; ++c) {
+          const int cb = S.cbit[c];
+          const bool low = ((lrank >> cb) & 1) == 0;  // this block holds the bit-0 half (a)
+          const C* rq = rmt(psi, lrank ^ (1 << cb));
           R a = (R)0;
           for (int e = tid; e < M; e += NT) {
             const C l = lam[swb(e, DBL)];
-            const C qr = remote(psi)[swb(e, DBL)];
-            // rank 0 holds the bit-0 half (a), rank 1 the bit-1 half (b)
-            if (S.caxis == 0)
+            const C qr = rq[swb(e, DBL)];
+            if (S.caxis[c] == 0)
               a += fma(l.x, qr.y, -l.y * qr.x);
             else
-              a += rank == 0 ? -fma(l.x, qr.x, l.y * qr.y) : fma(l.x, qr.x, l.y * qr.y);
+              a += low ? -fma(l.x, qr.x, l.y * qr.y) : fma(l.x, qr.x, l.y * qr.y);
           }
           a = wsum(a);
           if (lane == 0) S.red[warp][ns] = a * sc;
@@ -961,7 +1002,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
             else if (b < m)
               U = (b - LGNT == 0) ? Uk[0] : (b - LGNT == 1) ? Uk[1] : (b - LGNT == 2) ? Uk[2] : Uk[3];
             else
-              U = rank ? T : (R)0;
+              U = ((lrank >> (b - m)) & 1) ? T : (R)0;  // a top bit: fixed per block
             R val = wsum(T - (R)2 * U);
             if (lane == 0) S.red[warp][ns + j] = val * sc;
           }
@@ -972,8 +1013,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           if (tid < ns) {
             R tot = (R)0;
             for (int w = 0; w < NT / 32; ++w) tot += S.red[w][tid];
-            const int slot = tid < nxy ? S.xslot[tid] : (tid < nxy + ((CS > 1 && S.ncross) ? 1 : 0) ? S.cslot
-                                                                                                    : S.zslot[tid - nxy - ((CS > 1 && S.ncross) ? 1 : 0)]);
+            const int slot = tid < nxy ? S.xslot[tid] : tid < nxy + ncr ? S.cslot[tid - nxy] : S.zslot[tid - nxy - ncr];
             if (CS > 1)
               atomicAdd(&J.grad[slot], (double)tot);
             else
@@ -997,8 +1037,10 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           psi = rotate(lam, psi, true);
         else
           rotate_cross(lam, psi, true);
+        const bool fz = fuse && S.nz <= BZMAX;
+        if (fz && ladder) relabel();  // the fused table reads the new block's index
         build_diag(i, true);
-        if (fuse && S.nz <= BZMAX) {
+        if (fz) {
           entangle_diag(lam, true);
           entangle_diag(psi, true);
           if (CS > 1) cluster.sync();
@@ -1018,6 +1060,7 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           emit1(gsum, 2 * i + 1, 2.0);
         }
         if (J.kind == 0 && J.entangler != 0 && J.placement == 0) {
+          if (ladder) relabel();
           entangle(psi, true);
           entangle(lam, true);
         }
@@ -1058,6 +1101,18 @@ static cudaError_t launch_one(const BatchJob* jobs, int njobs, int* counter, int
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (CS > 1) {
+    // clusters co-resident at once (a cluster's CTAs share one GPC, which
+    // can leave SMs over); the job queue needs no co-residency, so this
+    // only avoids launching clusters that would wait for others to exit
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) == cudaSuccess && nc > 0 && nc < units) {
+      units = nc;
+      *grid_out = units;
+      cfg.gridDim = dim3(units * CS);
+    }
+    cudaGetLastError();
+  }
   e = cudaLaunchKernelEx(&cfg, kern, jobs, njobs, counter, mmax);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
@@ -1066,9 +1121,11 @@ static cudaError_t launch_one(const BatchJob* jobs, int njobs, int* counter, int
 cudaError_t launch_batched(int dtype_double, int cluster, const BatchJob* jobs, int njobs, int* counter, int mmax,
                            cudaStream_t st, int* grid_out) {
   if (dtype_double) {
+    if (cluster == 4) return launch_one<double, 4, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
     if (cluster == 2) return launch_one<double, 2, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
     return launch_one<double, 1, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
   }
+  if (cluster == 4) return launch_one<float, 4, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
   if (cluster == 2) return launch_one<float, 2, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
   return launch_one<float, 1, BATCH_THREADS>(jobs, njobs, counter, mmax, st, grid_out);
 }

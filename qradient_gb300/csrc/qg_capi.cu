@@ -1204,11 +1204,12 @@ int qg_batch_launch(int dtype, const qg_batch_job* jobs, int njobs, int max_qubi
   if (!jobs || !ws) return fail(QG_ERR_INVALID, "null pointer");
   if (wsb < 256) return fail(QG_ERR_WORKSPACE, "workspace %zu bytes < 256 needed", wsb);
   if (dtype != QG_C128 && dtype != QG_C64) return fail(QG_ERR_INVALID, "unknown dtype %d", dtype);
-  if (cluster != 1 && cluster != 2) return fail(QG_ERR_INVALID, "cluster must be 1 or 2");
+  if (cluster != 1 && cluster != 2 && cluster != 4) return fail(QG_ERR_INVALID, "cluster must be 1, 2 or 4");
   const int mlimit = dtype == QG_C128 ? BatchC<double>::MMAX : BatchC<float>::MMAX;
-  const int m = max_qubits - (cluster - 1);
+  const int lg = cluster == 4 ? 2 : cluster - 1;  // top bits split across the cluster
+  const int m = max_qubits - lg;
   if (max_qubits < 1 || m > mlimit)
-    return fail(QG_ERR_UNSUPPORTED, "batched jobs need n <= %d (cluster %d)", mlimit + cluster - 1, cluster);
+    return fail(QG_ERR_UNSUPPORTED, "batched jobs need n <= %d (cluster %d)", mlimit + lg, cluster);
   cudaStream_t st = (cudaStream_t)stream;
   QG_CUDA(cudaMemsetAsync(ws, 0, sizeof(int), st));
   int grid = 0;

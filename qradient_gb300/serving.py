@@ -36,7 +36,7 @@ import numpy as np
 import torch
 
 from . import _lib, _native
-from .batched import CLUSTER_MAX, Batch
+from .batched import CLUSTER_MAX, PAIR_MAX, SINGLE_MAX, Batch
 
 
 class Request:
@@ -83,7 +83,7 @@ class Server:
     """Admission by device-memory footprint, batched small requests, one
     stream per large request (up to ``streams`` concurrently)."""
 
-    def __init__(self, device=None, hbm_budget=None, streams=8, max_batch=4096, batch_streams=4,
+    def __init__(self, device=None, hbm_budget=None, streams=8, max_batch=4096, batch_streams=8,
                  history_share=0.5):
         self.device = _native.require_cuda(device)
         if hbm_budget is None:
@@ -234,13 +234,18 @@ class Server:
         return small, large
 
     def _launch_small(self, reqs):
-        by_dtype = collections.defaultdict(list)
+        # one batch per dtype and cluster size, each on the next batch stream:
+        # the launches of a round overlap instead of queueing behind the
+        # longest (4-CTA complex128 jobs, FP64-bound, run longest)
+        by_key = collections.defaultdict(list)
         for r in reqs:
-            by_dtype[r.dtype].append(r)
-        st = self.batch_streams[self._next_batch_stream]
-        self._next_batch_stream = (self._next_batch_stream + 1) % len(self.batch_streams)
-        with torch.cuda.stream(st):
-            for dt, rs in by_dtype.items():
+            n = r.circuit.qnum
+            cls = 1 if n <= SINGLE_MAX[r.dtype] else 2 if n <= PAIR_MAX[r.dtype] else 4
+            by_key[(r.dtype, cls)].append(r)
+        for (dt, _), rs in by_key.items():
+            st = self.batch_streams[self._next_batch_stream]
+            self._next_batch_stream = (self._next_batch_stream + 1) % len(self.batch_streams)
+            with torch.cuda.stream(st):
                 try:
                     b = Batch(device=self.device, dtype=dt, grad=any(r.op == "grad" for r in rs), use_graph=False)
                     for r in rs:
@@ -252,7 +257,7 @@ class Server:
                 except Exception as exc:  # the batch's requests fail, the server carries on
                     self._fail(rs, exc)
                     continue
-                self.inflight.append((ev, rs, b))
+            self.inflight.append((ev, rs, b))
 
     def _launch_large(self, r):
         idx = next(i for i, s in enumerate(self.stream_busy) if s is None)

@@ -58,6 +58,57 @@ def test_batch_mcclean_matches_oracle(dtype, tol):
         assert rel_err(g, g0) <= tol, (c.qnum, rel_err(g, g0))
 
 
+@pytest.mark.parametrize("dtype,tol,n", [("complex128", 1e-12, 14), ("complex64", 1e-4, 15)])
+def test_batch_four_cta_clusters_match_oracle(dtype, tol, n):
+    """Jobs above the 2-CTA limit run on 4-CTA clusters: the state split by
+    its top two qubits, cross-CTA rotations and reductions on both, and the
+    CNOT ladder's CNOT(0, 1) a relabelling of the blocks.  Every ladder form,
+    X and Y observable terms on both split qubits, QAOA, and a 2-CTA job in
+    the same batch, against the oracle."""
+    from qradient_gb300 import McClean, Qaoa
+    from qradient_gb300.batched import Batch
+    from qradient_gb300.optimization_problems import MaxCut, random_regular_edges
+
+    kind, q0, q1 = [3, 0, 1, 0, 1, 3], [0, 1, 0, 0, 1, 1], [1, 1, 0, 0, 1, n - 1]
+    w = [1.0, 0.3, -0.4, 0.2, 0.5, 0.6]
+    t = O.Terms(kind, q0, q1, w)
+    obs = obs_dict(n, np.array(kind), np.array(q0), np.array(q1), np.array(w))
+    b = Batch(dtype=dtype)
+    cases = []
+    for k, (L, ent, pl) in enumerate(((3, "cnot", "before"), (2, "cnot", "after"), (2, "cz", "after"),
+                                      (2, "cz", "before"), (2, None, "before"))):
+        rng = np.random.default_rng(200 + k)
+        axes = rng.integers(0, 3, (L, n))
+        angles = rng.uniform(0, 2 * np.pi, (L, n))
+        c = McClean(n, obs, L, axes=axes, angles=angles, entangler=ent, placement=pl, dtype=dtype)
+        b.add(c)
+        cases.append(("mc", c, axes, angles))
+    c2, axes2, angles2, t2 = _mc(n - 1, 2, 300, dtype=dtype)  # a 2-CTA job beside them
+    b.add(c2)
+    cases.append(("mc2", c2, axes2, angles2))
+    edges = random_regular_edges(3 if n % 2 == 0 else 4, n, 5)
+    q = Qaoa(n, MaxCut(n, edge_set=edges).to_observable(), 2, dtype=dtype)
+    rng = np.random.default_rng(5)
+    qp = np.stack([rng.uniform(0, np.pi, 2), rng.uniform(0, np.pi, 2)], axis=1)
+    b.add(q, params=qp)
+    cases.append(("qaoa", q, edges, qp))
+    E, G = b.grad()
+    assert not b._big and [g[0] for g in b._groups] == [2, 4], [g[0] for g in b._groups]
+    E = E.cpu().numpy()
+    for k, case in enumerate(cases):
+        if case[0] == "qaoa":
+            _, qc, ed, prm = case
+            tt = O.Terms(np.full(len(ed), 3), ed[:, 0], ed[:, 1], np.ones(len(ed)))
+            E0, g0 = O.qaoa_grad(n, prm[:, 0], prm[:, 1], tt)
+            g = G[k].cpu().numpy().reshape(-1, 2)
+        else:
+            _, c, axes, angles = case
+            E0, g0 = _oracle(c, axes, angles, t2 if case[0] == "mc2" else t)
+            g = G[k].cpu().numpy().reshape(g0.shape)
+        assert abs(E[k] - E0) <= tol * max(1.0, abs(E0)), (k, E[k], E0)
+        assert rel_err(g, g0) <= tol, (k, rel_err(g, g0))
+
+
 def test_batch_qaoa_and_mixed_sizes():
     """QAOA and McClean jobs of different sizes in one batch, including a
     circuit too large for shared memory (sweep path inside the same graph)."""

@@ -178,15 +178,16 @@ def test_sample_expec_val_is_unbiased(golden):
 def test_batched_term_expectations_and_shift_gradient():
     """The batched kernel's per-term expectations (the projector estimators'
     inputs) against qg_pauli_expectations on the same final states, for a
-    single-CTA complex128 job and a 2-CTA complex64 job with X, Y, Z and ZZ
-    terms; and the parameter-shift gradient through the batched launch
+    single-CTA complex128 job, 2-CTA and 4-CTA complex64 jobs and a 4-CTA
+    complex128 job with X, Y, Z and ZZ terms (X and Y on the split qubits); and the parameter-shift gradient through the batched launch
     against the per-circuit path (forced by an explicit |0..0> start)."""
     import torch
 
     from qradient_gb300 import McClean
     from qradient_gb300.batched import Batch
 
-    for n, L, dtype, tol in ((10, 3, "complex128", 1e-12), (14, 2, "complex64", 2e-5)):
+    for n, L, dtype, tol in ((10, 3, "complex128", 1e-12), (14, 2, "complex64", 2e-5), (14, 2, "complex128", 1e-12),
+                             (15, 2, "complex64", 2e-5)):
         rng = np.random.default_rng(n)
         obs = {"zz": np.full((n, n), None), "x": np.full(n, None), "y": np.full(n, None), "z": np.full(n, None)}
         obs["zz"][0, 1] = 0.7
