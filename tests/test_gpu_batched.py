@@ -265,8 +265,8 @@ def test_config3_full_batch_and_complex128_check():
     sampled jobs against the FP64 oracle (the reference's grad_run
     restated, mc_clean.py:47-78) and against central differences (h =
     1e-5) of complex128 runs; and the complex128 check: n=14 complex128 jobs
-    exceed the 2-CTA limit (13), so they run on the sweep path inside the
-    same graph, checked against the oracle to 1e-12."""
+    exceed the 2-CTA limit (13) and run on 4-CTA clusters of the same
+    kernel, in one graph replay, checked against the oracle to 1e-12."""
     import torch
 
     from qradient_gb300 import McClean
@@ -307,9 +307,10 @@ def test_config3_full_batch_and_complex128_check():
             assert abs(G[k, i, q] - g0[i, q]) <= 1e-4 * max(1.0, np.max(np.abs(g0)))
     print("config 3, 4096 vectors, complex64: worst normwise gradient error of 6 sampled jobs vs FP64 %.2e" % worst)
     assert worst <= 1e-4
-    # the complex128 check (the sweep path inside the graph)
+    # the complex128 check (4-CTA clusters)
     B2 = 32
     b2 = mcclean_batch(n, L, axes, {"zz": zz}, B2, dtype="complex128")
+    assert not b2._big and [g[0] for g in b2._groups] == [4]
     b2.params_flat.copy_(torch.as_tensor(P[:B2].reshape(-1), device=b2.params_flat.device))
     b2.grad()
     E2, _ = b2.grad()
