@@ -28,6 +28,7 @@ The default run adds, measured in the same process after the headline:
              HBM: the uncompute form of the adjoint sweep)
   batched    4096 parameter vectors of McClean n=14 L=30 complex64 in one
              CUDA-graph replay, against the plain per-call path
+  batched_c128  the same circuit in complex128, 1024 vectors (4-CTA clusters)
   served     Poisson streams through the continuous-batching server (the
              n <= 14 share of the request population and the full n <= 26
              population), against the plain per-call path
@@ -806,6 +807,8 @@ def main():
         # the largest configured size whose history does not fit: uncompute mode
         line["large"] = measure_mcclean(28, 50, 28, "complex128", "cnot", "before", 2, 2, dev, min_warmup=2)
         line["batched"] = measure_batched(14, 30, 4096, "complex64", 5, 3, 14, dev, e2e=True)
+        # config 3's complex128 check: n = 14 complex128 jobs on 4-CTA clusters
+        line["batched_c128"] = measure_batched(14, 30, 1024, "complex128", 3, 3, 14, dev, e2e=False)
         line["served"] = {"small": measure_served(24, 1000, 14, args.streams, dev),
                           "full": measure_served(26, 60, 26, args.streams, dev)}
         line["extras_clocks"] = extra_clk.stop()
