@@ -264,7 +264,8 @@ int qg_batch_workspace_size(size_t* bytes);
  * must share dtype; max_qubits bounds their n (sets the shared-memory size).
  * cluster: CTAs per job, 1, 2 or 4 (the state split by its top 0, 1 or 2
  * bits): one CTA holds complex64 n <= 13 / complex128 n <= 12, two one
- * qubit more, four two more.  4-CTA jobs add their partial sums with atomic
+ * qubit more, four two more.  A job whose n exceeds max_qubits, or leaves a
+ * cluster's CTA fewer than 2 qubits, gets NaN outputs.  4-CTA jobs add their partial sums with atomic
  * adds in arrival order (their outputs can vary in the last bit). */
 int qg_batch_launch(int dtype, const qg_batch_job* jobs_dev, int njobs, int max_qubits, int cluster,
                     void* workspace_dev, size_t workspace_bytes, qg_stream stream);

@@ -423,6 +423,19 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
     scr = buf0 + 2 * Mmax;
     const int n = J.n;
     const int m = n - LGCS;
+    if (m < (CS > 1 ? 2 : 1) || m > mmax || J.layers < 0) {
+      // a job this launch cannot hold (its block would overrun the shared
+      // memory sized for mmax, or leave a cluster's CTA fewer than 2 bits):
+      // NaN outputs, no state touched; the decision is the same in every CTA
+      if (tid == 0 && rank == 0) {
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        if (J.expec) *J.expec = nan;
+        if (J.grad && J.layers >= 0)
+          for (int i = 0, np = J.kind == 0 ? J.layers * n : 2 * J.layers; i < np; ++i) J.grad[i] = nan;
+      }
+      csync();  // every thread has read S.job before the next fetch rewrites it
+      continue;
+    }
     const int M = 1 << m;
     hflip = 0;
     int lrank = rank;  // logical rank: the top bits of this CTA's block

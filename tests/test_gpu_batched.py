@@ -319,3 +319,33 @@ def test_config3_full_batch_and_complex128_check():
     for k in (0, B2 - 1):
         E0, g0 = O.mcclean_grad(n, axes, P[k].reshape(L, n), t)
         assert abs(E2[k].item() - E0) <= 1e-12 and rel_err(G2[k], g0) <= 1e-12, (k, rel_err(G2[k], g0))
+
+
+def test_batch_launch_marks_jobs_it_cannot_hold():
+    """qg_batch_launch sizes shared memory by max_qubits; a job above it is
+    not run (the kernel checks each job) and gets NaN outputs, the others
+    run as usual."""
+    import math
+
+    import torch
+
+    from qradient_gb300 import _lib, _native
+    from qradient_gb300.batched import Batch
+
+    b = Batch(dtype="complex64", use_graph=False)
+    (c1, ax1, an1, t1), (c2, _, _, _) = _mc(8, 2, 1, dtype="complex64"), _mc(10, 2, 2, dtype="complex64")
+    b.add(c1)
+    b.add(c2)
+    b.finalize()
+    assert [g[0] for g in b._groups] == [1]
+    cl, jobs, nj, maxq, ws = b._groups[0]
+    lib = _lib.load()
+    _lib.check(lib.qg_batch_launch(_lib.QG_C64, _native.ptr(jobs), nj, 8, cl, _native.ptr(ws), ws.numel(),
+                                   _native.stream_handle(b.device)))
+    torch.cuda.synchronize()
+    E = b.expec.cpu().numpy()
+    E0, g0 = _oracle(c1, ax1, an1, t1)
+    assert abs(E[0] - E0) <= 1e-4 and math.isnan(E[1])
+    G = b.grads_flat.cpu().numpy()
+    assert rel_err(G[: g0.size].reshape(g0.shape), g0) <= 1e-4
+    assert np.all(np.isnan(G[g0.size: g0.size + 20]))
