@@ -58,7 +58,6 @@ class Batch:
         self.use_graph = use_graph
         self.cluster_from = SINGLE_MAX[self.dtype] + 1 if cluster_from is None else int(cluster_from)
         self._specs = []
-        self._keep = []
         self._graph = None
         self._views = None
         self.finalized = False

@@ -41,7 +41,7 @@ from .batched import CLUSTER_MAX, PAIR_MAX, SINGLE_MAX, Batch
 
 class Request:
     __slots__ = ("rid", "circuit", "params", "op", "dtype", "t_arrival", "t_done", "expec", "grad", "state",
-                 "footprint", "error", "_e", "_g", "_event", "_keep", "_gop")
+                 "footprint", "error", "_e", "_g", "_gop")
 
     def __init__(self, rid, circuit, params, op="grad", dtype="complex128", t_arrival=None):
         self.rid = rid
@@ -58,8 +58,6 @@ class Request:
         self.footprint = 0
         self.error = None
         self._e = self._g = None
-        self._event = None
-        self._keep = None
         self._gop = None
 
     @property
