@@ -40,7 +40,7 @@ from .batched import CLUSTER_MAX, PAIR_MAX, SINGLE_MAX, Batch
 
 
 class Request:
-    __slots__ = ("rid", "circuit", "params", "op", "dtype", "t_arrival", "t_done", "expec", "grad", "state",
+    __slots__ = ("rid", "circuit", "params", "op", "dtype", "t_arrival", "t_done", "expec", "grad",
                  "footprint", "error", "_e", "_g", "_gop")
 
     def __init__(self, rid, circuit, params, op="grad", dtype="complex128", t_arrival=None):
