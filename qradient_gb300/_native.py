@@ -84,10 +84,10 @@ class NativeCircuit:
         L = axes.size // n if n else 0
         kind, q0, q1, w = terms
         h = ctypes.c_void_p()
-        _lib.check(lib.qg_mcclean_create(n, L, axes.ctypes.data_as(ctypes.c_void_p), entangler, placement,
-                                         len(kind), kind.ctypes.data_as(ctypes.c_void_p),
-                                         q0.ctypes.data_as(ctypes.c_void_p), q1.ctypes.data_as(ctypes.c_void_p),
-                                         w.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)))
+        _lib.check(lib.qg_mcclean_create(n, L, axes.ctypes.data, entangler, placement,
+                                         len(kind), kind.ctypes.data,
+                                         q0.ctypes.data, q1.ctypes.data,
+                                         w.ctypes.data, ctypes.byref(h)))
         return cls(h, 0, n, L)
 
     @classmethod
@@ -95,9 +95,9 @@ class NativeCircuit:
         lib = _lib.load()
         kind, q0, q1, w = terms
         h = ctypes.c_void_p()
-        _lib.check(lib.qg_qaoa_create(n, p, len(kind), kind.ctypes.data_as(ctypes.c_void_p),
-                                      q0.ctypes.data_as(ctypes.c_void_p), q1.ctypes.data_as(ctypes.c_void_p),
-                                      w.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)))
+        _lib.check(lib.qg_qaoa_create(n, p, len(kind), kind.ctypes.data,
+                                      q0.ctypes.data, q1.ctypes.data,
+                                      w.ctypes.data, ctypes.byref(h)))
         return cls(h, 1, n, p)
 
     def __del__(self):

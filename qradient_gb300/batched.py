@@ -274,10 +274,10 @@ class Batch:
             lib = _lib.load()
             out = np.zeros(600, dtype=_COST)
             nout, w0, maxabs = ctypes.c_int(0), ctypes.c_double(0), ctypes.c_int(0)
-            status = lib.qg_qaoa_cost_terms(c.qnum, len(kindv), kindv.ctypes.data_as(ctypes.c_void_p),
-                                            q0.ctypes.data_as(ctypes.c_void_p), q1.ctypes.data_as(ctypes.c_void_p),
-                                            w.ctypes.data_as(ctypes.c_void_p), 600,
-                                            out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nout),
+            status = lib.qg_qaoa_cost_terms(c.qnum, len(kindv), kindv.ctypes.data,
+                                            q0.ctypes.data, q1.ctypes.data,
+                                            w.ctypes.data, 600,
+                                            out.ctypes.data, ctypes.byref(nout),
                                             ctypes.byref(w0), ctypes.byref(maxabs))
             if status != _lib.QG_OK or maxabs.value > MAX_COST:
                 return None  # not representable in the batched kernel: sweep path
