@@ -811,7 +811,8 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         build_diag(i, false);
         apply_diag(psi, false);
       }
-      if (CS > 1) cluster.sync();
+      // (no cluster barrier here: the only cross-CTA reads of a layer,
+      // rotate_cross's, sit between barriers of their own)
       rotate(psi, nullptr, false);
       if (J.kind == 0 && J.entangler != 0 && J.placement == 1) {
         if (ladder) relabel();
@@ -936,7 +937,6 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           if (ladder) relabel();
           entangle(psi, true);
           entangle(lam, true);
-          if (CS > 1) cluster.sync();
         }
         // gradient reductions of the X/Y rotations on local bits fused with
         // their inverses on lam and psi; per-warp sums in S.red[warp][k].
@@ -1043,8 +1043,9 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
             J.grad[2 * i] = (double)tot;
         }
         __syncthreads();
-        // the partner may still read this CTA's psi for its top-bit reduction
-        if (CS > 1) cluster.sync();
+        // complex128 rotates psi here before rotate_cross's first barrier:
+        // the partners may still read it for their cross reductions
+        if (CS > 1 && DBL && ncr) cluster.sync();
         // inverse rotations on lam and psi
         if (DBL)
           psi = rotate(lam, psi, true);
@@ -1056,7 +1057,6 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
         if (fz) {
           entangle_diag(lam, true);
           entangle_diag(psi, true);
-          if (CS > 1) cluster.sync();
           continue;
         }
         apply_diag(lam, true);
@@ -1077,7 +1077,9 @@ __global__ void __launch_bounds__(NT, 1) batched_kernel(const BatchJob* __restri
           entangle(psi, true);
           entangle(lam, true);
         }
-        if (CS > 1) cluster.sync();
+        // (no end-of-layer cluster barrier: every cross-CTA read of the
+        // layer ended at rotate_cross's last barrier, and the next layer's
+        // first cross read (its reductions) waits at a barrier of its own)
       }
     }
     csync();
